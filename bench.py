@@ -1,0 +1,329 @@
+#!/usr/bin/env python
+"""EBSD pattern synthesis throughput on GB300.
+
+Workload: the production plain-forward case -- a 640x480 detector (20 um
+pixels, L = 15000 um, xpc = 1.5, ypc = -3.0 px, tilt 10 deg, gamma 0.33) on a
+1001^2 x 11-bin Ni master pattern (10-20 keV), 10 000 uniformly random
+orientations (Shoemake, seed 1).  Inputs are seeded synthetic stand-ins in
+the reference's formats (the reference ships no data).
+
+A step is one pass of the pattern loop over the 10 000 orientations (one
+kernel launch).  `value` is patterns/s with the master, detector weights,
+quaternions and the 12.3 GB of output resident in HBM; L2 is flushed between
+timed steps.  `e2e` is the same metric through the C ABI with host buffers
+(quaternions uploaded from pinned memory, patterns copied back to pinned
+memory each step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank computes its own 10 000 orientations
+(weak scaling, no collective on the data path); rank 0 prints one JSON line.
+`--impl reference` times the CPU restatement of the reference loop on the
+host cores (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "EBSD patterns/s 640x480 (plain forward), 1001^2 x 11-bin master"
+UNIT = "patterns/s"
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--orient", type=int, default=10000)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_pattern():
+    """DRAM bytes per pattern of the pattern kernel from the committed ncu
+    summary (profiles/), or None."""
+    f = ROOT / "profiles" / "k_forward_640x480.md"
+    if not f.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_pattern\s*=\s*([0-9.eE+]+)", f.read_text())
+    return float(m.group(1)) if m else None
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            self.fh = os.fdopen(fd, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _setup_data(rank: int, n: int):
+    from ctemsoft_gb300 import synth
+    wl = synth.C2
+    sr, acc = wl.master(), wl.mc()
+    q = synth.shoemake_quaternions(n, wl.seed + 7919 * rank)
+    return wl, sr, acc, q
+
+
+def cpu_baseline(wl, sr, acc, q, seconds: float, per_step: int | None = None, steps: int = 1,
+                 warmup: int = 0):
+    """Time the oracle's FP32 restatement of the loop on all host threads
+    over a bounded sample of the orientations."""
+    from oracle import oracle as O
+    threads = O.max_threads()
+    Emin, Emax = 1, wl.nEbins
+    det = O.Detector(wl.geometry(), acc, Emin, Emax)
+    pref = O.prefactor(wl.beamcurrent, wl.dwelltime, det.num_el)
+    t = time.perf_counter()
+    det.patterns_f32(sr, q[:1], pref, nthreads=1)
+    t1 = time.perf_counter() - t
+    if per_step is None:
+        per_step = int(max(threads, min(len(q), round(seconds * threads / max(t1, 1e-6)))))
+    per_step = min(per_step, len(q))
+    for w in range(warmup):
+        det.patterns_f32(sr, q[:threads], pref, nthreads=threads)
+    total = 0.0
+    done = 0
+    for s in range(steps):
+        lo = (s * per_step) % max(1, len(q) - per_step + 1)
+        t = time.perf_counter()
+        det.patterns_f32(sr, q[lo:lo + per_step], pref, nthreads=threads)
+        total += time.perf_counter() - t
+        done += per_step
+    return {"value": done / total, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{per_step} of {len(q)} orientations x {steps} step(s), "
+                      f"640x480, FP32 oracle restatement, OpenMP over orientations",
+            "single_thread_patterns_per_s": 1.0 / t1}
+
+
+def run_reference(args):
+    rank, world, local = _dist()
+    if rank != 0:
+        return 0
+    wl, sr, acc, q = _setup_data(0, args.orient)
+    from oracle import oracle as O
+    threads = O.max_threads()
+    base = cpu_baseline(wl, sr, acc, q, 0.0, per_step=4 * threads, steps=args.steps,
+                        warmup=args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * (4 * threads) / base["value"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": synth_name(), "orientations": args.orient,
+                   "detector": "640x480", "master": "1001x1001x11"},
+        "cpu_baseline": base,
+        "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def synth_name():
+    from ctemsoft_gb300 import synth
+    return synth.C2.name
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from ctemsoft_gb300 import capi
+
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl, sr, acc, q = _setup_data(rank, args.orient)
+    N = len(q)
+
+    h = capi.Handle(local)
+    h.set_master(sr)
+    num_el = h.set_detector(wl.geometry(), acc, 1, wl.nEbins)
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    epi = capi.epilogue(pref, binning=1, scalingmode="gam", gammavalue=wl.gammavalue)
+    nx, ny = h.output_dims(epi)
+    P = wl.numsx * wl.numsy
+
+    stream = torch.cuda.current_stream(dev)
+    h.set_stream(stream.cuda_stream)
+    dq = torch.from_numpy(q).to(dev)
+    dout = torch.empty((N, ny, nx), dtype=torch.float32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        h.forward(dq, epi, out=dout)
+    barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()  # evict L2 between timed steps (outside the events)
+        ev[k][0].record(stream)
+        h.forward(dq, epi, out=dout)
+        ev[k][1].record(stream)
+    barrier()
+    ck = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([tot_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = world * N * args.steps / (tot_ms / 1000.0)
+    launch_ms = statistics.mean(step_ms)
+
+    # end to end through the C ABI with host buffers
+    del dout
+    torch.cuda.empty_cache()
+    hq = torch.empty((N, 4), dtype=torch.float32, pin_memory=True)
+    hq.copy_(torch.from_numpy(q))
+    hout = torch.empty((N, ny, nx), dtype=torch.float32, pin_memory=True)
+    h.set_stream(None)
+    h.forward(hq, epi, out=hout)  # warm-up
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        h.forward(hq, epi, out=hout)
+        _ = float(hout[N - 1, ny - 1, nx - 1])  # result is on the host
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_val = world * N * args.e2e_steps / e2e_s
+    ok = bool(np.isfinite(hout[0].numpy()).all())
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(wl, sr, acc, q, args.cpu_seconds)
+
+    if rank == 0:
+        peak, peak_kind = _peaks()
+        b_pattern = P * (16 * wl.nEbins + 4)
+        achieved = b_pattern * N / (launch_ms / 1000.0) / 1e9
+        tpp = _traffic_per_pattern()
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded stand-ins in the reference's file formats)",
+            "config": {"workload": wl.name, "detector": f"{wl.numsx}x{wl.numsy}",
+                       "master": f"{2 * wl.npx + 1}^2 x {wl.nEbins} bins",
+                       "orientations_per_gpu": N, "epilogue": "prefactor, gamma 0.33",
+                       "l2": "flushed (512 MB write) between timed steps",
+                       "parallelism": f"orientation shards x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": (tpp * N if tpp else None),
+                         "algorithmic_bytes_per_pattern": b_pattern,
+                         "note": "gathered master bytes are served by L1/L2 (master is "
+                                 "L2-resident), so frac can exceed 1"},
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(N * 16),
+                    "d2h_bytes_per_step": int(N * nx * ny * 4), "steps": args.e2e_steps,
+                    "finite": ok},
+            "gpu_launches": args.steps,
+            "clocks": ck,
+            "cpu_baseline": base,
+        }
+        print(json.dumps(line))
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = _args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,307 @@
+"""ctypes binding of libebsdgpu.so (include/ebsd_gpu.h).
+
+This is the Python face of the C ABI: the same entry points, argument
+meanings and error codes, with numpy arrays in place of raw pointers.  There
+is no fallback: if the library is missing, importing the binding fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libebsdgpu.so"
+
+EBSD_OK = 0
+EBSD_EINVAL = -1
+EBSD_ECUDA = -2
+EBSD_ENOMEM = -3
+EBSD_ESTATE = -4
+EBSD_EIO = -5
+EBSD_EFORMAT = -6
+EBSD_EUNSUPPORTED = -7
+EBSD_ETIMEOUT = -8
+
+SCALING = {"not": 0, "lin": 1, "gam": 2}
+
+
+class EBSDError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{msg} (code {code})")
+        self.code = code
+
+
+class Geometry(C.Structure):
+    _fields_ = [("L", C.c_float), ("thetac", C.c_float), ("delta", C.c_float),
+                ("numsx", C.c_int32), ("numsy", C.c_int32), ("xpc", C.c_float),
+                ("ypc", C.c_float), ("sig", C.c_double)]
+
+
+class Epilogue(C.Structure):
+    _fields_ = [("prefactor", C.c_double), ("binning", C.c_int32), ("scalingmode", C.c_int32),
+                ("gammavalue", C.c_float), ("poisson", C.c_int32), ("seed", C.c_uint64)]
+
+
+class MCHeader(C.Structure):
+    _fields_ = [("numEbins", C.c_int32), ("numzbins", C.c_int32), ("numsx", C.c_int32),
+                ("numsy", C.c_int32), ("num_el_total", C.c_int64), ("nthreads", C.c_int32),
+                ("EkeV", C.c_double), ("Ehistmin", C.c_double), ("Ebinsize", C.c_double),
+                ("depthmax", C.c_double), ("depthstep", C.c_double), ("sig", C.c_double),
+                ("omega", C.c_double), ("MCmode", C.c_char * 5)]
+
+
+class MasterHeader(C.Structure):
+    _fields_ = [("npx", C.c_int32), ("npy", C.c_int32), ("nE", C.c_int32),
+                ("numset", C.c_int32), ("sqorhe", C.c_char * 7)]
+
+
+class Namelist(C.Structure):
+    _fields_ = [("L", C.c_float), ("thetac", C.c_float), ("delta", C.c_float),
+                ("numsx", C.c_int32), ("numsy", C.c_int32), ("xpc", C.c_float),
+                ("ypc", C.c_float), ("anglefile", C.c_char * 512),
+                ("eulerconvention", C.c_char * 4), ("FZfile", C.c_char * 512),
+                ("energyfile", C.c_char * 512), ("datafile", C.c_char * 512),
+                ("beamcurrent", C.c_double), ("dwelltime", C.c_double),
+                ("energymin", C.c_float), ("energymax", C.c_float), ("binning", C.c_int32),
+                ("gammavalue", C.c_float), ("scalingmode", C.c_char * 4),
+                ("axisangle", C.c_float * 4), ("poisson", C.c_int32), ("seed", C.c_int64)]
+
+
+_P = C.c_void_p
+_SIGS = {
+    "ebsd_version": (C.c_int, []),
+    "ebsd_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "ebsd_destroy": (None, [_P]),
+    "ebsd_last_error": (C.c_char_p, [_P]),
+    "ebsd_set_stream": (C.c_int, [_P, _P]),
+    "ebsd_set_option": (C.c_int, [_P, C.c_char_p, C.c_int64]),
+    "ebsd_set_master": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "ebsd_set_detector": (C.c_int, [_P, C.POINTER(Geometry), _P, C.c_int32, C.c_int32,
+                                    C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
+    "ebsd_energy_window": (C.c_int, [C.c_float, C.c_float, C.c_double, C.c_double, C.c_int32,
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ebsd_prefactor": (C.c_double, [C.c_double, C.c_double, C.c_int32]),
+    "ebsd_output_dims": (C.c_int, [_P, C.POINTER(Epilogue), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32)]),
+    "ebsd_forward": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P]),
+    "ebsd_cells": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P, _P]),
+    "ebsd_get_detector": (C.c_int, [_P, _P, _P, _P, _P]),
+    "ebsd_run_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
+    "ebsd_read_mc_file": (C.c_int, [C.c_char_p, C.POINTER(MCHeader), _P]),
+    "ebsd_read_master_file": (C.c_int, [C.c_char_p, C.POINTER(MasterHeader), _P, _P, _P]),
+    "ebsd_read_namelist": (C.c_int, [C.c_char_p, C.POINTER(Namelist)]),
+    "ebsd_read_angle_file": (C.c_int, [C.c_char_p, C.c_char_p, _P, C.POINTER(C.c_int64), _P]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libebsdgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() or "
+                              "python ctemsoft_gb300/build.py")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def _check(rc: int, handle=None) -> None:
+    if rc != EBSD_OK:
+        msg = lib().ebsd_last_error(handle).decode(errors="replace")
+        raise EBSDError(rc, msg)
+
+
+def _ptr(a) -> int | None:
+    """Raw address of a numpy array, a torch tensor, or an int."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+def energy_window(energymin, energymax, Ehistmin, Ebinsize, numEbins):
+    a, b = C.c_int32(), C.c_int32()
+    _check(lib().ebsd_energy_window(energymin, energymax, Ehistmin, Ebinsize, numEbins,
+                                    C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def prefactor(beamcurrent, dwelltime, num_el):
+    return lib().ebsd_prefactor(beamcurrent, dwelltime, num_el)
+
+
+def epilogue(prefactor=1.0, binning=1, scalingmode="not", gammavalue=1.0, poisson=False,
+             seed=1) -> Epilogue:
+    mode = SCALING[scalingmode] if isinstance(scalingmode, str) else int(scalingmode)
+    return Epilogue(prefactor, binning, mode, gammavalue, int(bool(poisson)), seed)
+
+
+class Handle:
+    """One device, one stream, the master pattern and one detector."""
+
+    def __init__(self, device: int = 0):
+        self._h = _P()
+        _check(lib().ebsd_create(C.byref(self._h), device))
+        self.num_el = None
+        self.geometry = None
+
+    def close(self):
+        if self._h:
+            lib().ebsd_destroy(self._h)
+            self._h = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def raw(self):
+        return self._h
+
+    def set_stream(self, stream_ptr: int | None):
+        _check(lib().ebsd_set_stream(self._h, stream_ptr), self._h)
+
+    def set_option(self, key: str, value: int):
+        _check(lib().ebsd_set_option(self._h, key.encode(), int(value)), self._h)
+
+    def set_master(self, srtmp: np.ndarray):
+        """srtmp: array shaped (numset, nE, 2npy+1, 2npx+1), i.e. the Fortran
+        srtmp(-npx:npx,-npy:npy,nE,numset) in C order (x fastest)."""
+        sr = np.ascontiguousarray(srtmp, dtype=np.float32)
+        if sr.ndim == 3:
+            sr = sr[None]
+        numset, nE, gy, gx = sr.shape
+        _check(lib().ebsd_set_master(self._h, _ptr(sr), (gx - 1) // 2, (gy - 1) // 2, nE, numset),
+               self._h)
+
+    def set_detector(self, geom: dict, accum_e: np.ndarray, Emin: int, Emax: int) -> int:
+        """accum_e: array shaped (2nsy+1, 2nsx+1, numEbins) = Fortran
+        accum_e(numEbins,-nsx:nsx,-nsy:nsy).  Returns num_el."""
+        acc = np.ascontiguousarray(accum_e, dtype=np.int32)
+        gy, gx, nE = acc.shape
+        g = Geometry(geom["L"], geom["thetac"], geom["delta"], geom["numsx"], geom["numsy"],
+                     geom["xpc"], geom["ypc"], geom["sig"])
+        ne = C.c_int32()
+        _check(lib().ebsd_set_detector(self._h, C.byref(g), _ptr(acc), (gx - 1) // 2,
+                                       (gy - 1) // 2, nE, Emin, Emax, C.byref(ne)), self._h)
+        self.num_el = ne.value
+        self.geometry = dict(geom)
+        return ne.value
+
+    def output_dims(self, epi: Epilogue):
+        nx, ny = C.c_int32(), C.c_int32()
+        _check(lib().ebsd_output_dims(self._h, C.byref(epi), C.byref(nx), C.byref(ny)), self._h)
+        return nx.value, ny.value
+
+    def forward(self, quats, epi: Epilogue, out=None):
+        """Patterns for quats (n x 4, scalar first).  quats/out may be numpy
+        arrays (host) or torch CUDA tensors (device).  Returns out shaped
+        (n, ny, nx)."""
+        n = int(quats.shape[0])
+        nx, ny = self.output_dims(epi)
+        if isinstance(quats, np.ndarray):
+            quats = np.ascontiguousarray(quats, dtype=np.float32)
+        if out is None:
+            out = np.empty((n, ny, nx), dtype=np.float32)
+        _check(lib().ebsd_forward(self._h, _ptr(quats), n, C.byref(epi), _ptr(out)), self._h)
+        return out
+
+    def cells(self, quats: np.ndarray):
+        q = np.ascontiguousarray(quats, dtype=np.float32)
+        n = q.shape[0]
+        ny, nx = self.geometry["numsy"], self.geometry["numsx"]
+        nix = np.empty((n, ny, nx), np.int32)
+        niy = np.empty_like(nix)
+        i0 = np.empty((n, ny, nx), np.float32)
+        i1 = np.empty_like(i0)
+        _check(lib().ebsd_cells(self._h, _ptr(q), n, _ptr(nix), _ptr(niy), _ptr(i0), _ptr(i1)),
+               self._h)
+        return nix, niy, i0, i1
+
+    def get_detector(self, nE: int):
+        ny, nx = self.geometry["numsy"], self.geometry["numsx"]
+        W = np.empty((ny, nx, nE), np.float32)
+        rgx = np.empty((ny, nx), np.float32)
+        rgy = np.empty_like(rgx)
+        rgz = np.empty_like(rgx)
+        _check(lib().ebsd_get_detector(self._h, _ptr(W), _ptr(rgx), _ptr(rgy), _ptr(rgz)),
+               self._h)
+        return W, rgx, rgy, rgz
+
+
+def run_namelist(path: str, device: int = 0, quiet: bool = True) -> None:
+    _check(lib().ebsd_run_namelist(str(path).encode(), device, int(quiet)))
+
+
+def read_mc_file(path: str, with_data: bool = True):
+    h = MCHeader()
+    _check(lib().ebsd_read_mc_file(str(path).encode(), C.byref(h), None))
+    if not with_data:
+        return h, None
+    nsx, nsy = (h.numsx - 1) // 2, (h.numsy - 1) // 2
+    acc = np.empty((2 * nsy + 1, 2 * nsx + 1, h.numEbins), np.int32)
+    _check(lib().ebsd_read_mc_file(str(path).encode(), C.byref(h), _ptr(acc)))
+    return h, acc
+
+
+def read_master_file(path: str, with_data: bool = True):
+    h = MasterHeader()
+    _check(lib().ebsd_read_master_file(str(path).encode(), C.byref(h), None, None, None))
+    ek = np.empty(h.nE, np.float32)
+    at = np.empty(h.numset, np.int32)
+    sr = None
+    if with_data:
+        sr = np.empty((h.numset, h.nE, 2 * h.npy + 1, 2 * h.npx + 1), np.float32)
+    _check(lib().ebsd_read_master_file(str(path).encode(), C.byref(h), _ptr(ek), _ptr(at),
+                                       _ptr(sr)))
+    return h, ek, at, sr
+
+
+def read_namelist(path: str) -> dict:
+    n = Namelist()
+    _check(lib().ebsd_read_namelist(str(path).encode(), C.byref(n)))
+    out = {}
+    for name, _ in Namelist._fields_:
+        v = getattr(n, name)
+        if isinstance(v, bytes):
+            v = v.decode()
+        elif name == "axisangle":
+            v = list(v)
+        out[name] = v
+    return out
+
+
+def read_angle_file(path: str, eulerconvention: str = "tsl", axisangle=(0, 0, 0, 0)):
+    aa = (C.c_float * 4)(*axisangle)
+    n = C.c_int64(0)
+    _check(lib().ebsd_read_angle_file(str(path).encode(), eulerconvention.encode(), aa,
+                                      C.byref(n), None))
+    q = np.empty((n.value, 4), np.float32)
+    _check(lib().ebsd_read_angle_file(str(path).encode(), eulerconvention.encode(), aa,
+                                      C.byref(n), _ptr(q)))
+    return q

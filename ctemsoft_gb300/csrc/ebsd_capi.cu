@@ -1,0 +1,700 @@
+// C ABI of libebsdgpu.so: handle life cycle, set-up stages and the pattern
+// loop with host or device buffers.  See include/ebsd_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ebsd_host.h"
+#include "ebsd_internal.h"
+
+using namespace ebsd;
+
+struct ebsd_handle {
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;   // where work is issued
+    cudaStream_t copy_stream = nullptr;
+    std::string err;
+
+    // master: raw Fortran-order sr summed over nothing yet (all sets)
+    float* d_master_raw = nullptr;
+    int npx = 0, npy = 0, nE = 0, numset = 0;
+    bool have_master = false;
+    float max_sr = 0.0f;
+
+    // energy-interleaved master for the current window
+    float4* d_master_il = nullptr;
+    size_t il_bytes = 0;
+    int il_e0 = -1, il_nsel = 0;
+
+    // detector
+    bool have_detector = false;
+    ebsd_geometry geom{};
+    int Emin = 0, Emax = 0, nsel = 0, NV = 0;
+    int32_t num_el = 0;
+    float4* d_rg = nullptr;
+    float4* d_W = nullptr;
+    int P = 0;
+
+    // per-call buffers
+    DeviceBuf quats[2];
+    DeviceBuf outb[2];
+    DeviceBuf tmp;
+    float* pinned[2] = {nullptr, nullptr};
+    size_t pinned_bytes = 0;
+    cudaEvent_t ev_comp[2] = {nullptr, nullptr};
+    cudaEvent_t ev_d2h[2] = {nullptr, nullptr};
+
+    // L2 persistence
+    int max_persist = 0, max_window = 0;
+
+    LaunchCfg cfg;
+    int weights_fp64 = 1;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(ebsd_handle* h, int code, const char* fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (h)
+        h->err = buf;
+    else
+        g_err = buf;
+    return code;
+}
+
+int cuda_err(ebsd_handle* h, cudaError_t e, const char* what)
+{
+    return set_err(h, e == cudaErrorMemoryAllocation ? EBSD_ENOMEM : EBSD_ECUDA, "%s: %s", what,
+                   cudaGetErrorString(e));
+}
+
+#define CK(h, call, what)                                  \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_err(h, e_, what); \
+    } while (0)
+
+int ensure(ebsd_handle* h, DeviceBuf& b, size_t bytes, const char* what)
+{
+    if (b.bytes >= bytes) return EBSD_OK;
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(h, EBSD_ENOMEM, "cudaMalloc %zu bytes for %s: %s", bytes, what,
+                       cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    return EBSD_OK;
+}
+
+enum PtrKind { kPageable = 0, kPinned = 1, kDevice = 2 };
+
+PtrKind ptr_kind(const void* p)
+{
+    cudaPointerAttributes a;
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return kPageable;
+    }
+    switch (a.type) {
+        case cudaMemoryTypeDevice:
+        case cudaMemoryTypeManaged: return kDevice;
+        case cudaMemoryTypeHost: return kPinned;
+        default: return kPageable;
+    }
+}
+
+int activate(ebsd_handle* h)
+{
+    CK(h, cudaSetDevice(h->device), "cudaSetDevice");
+    return EBSD_OK;
+}
+
+// Parallel host copy (pinned staging -> pageable user buffer).
+void parallel_memcpy(void* dst, const void* src, size_t bytes)
+{
+    const size_t min_chunk = size_t(8) << 20;
+    unsigned hw = std::thread::hardware_concurrency();
+    unsigned nt = (unsigned)std::min<size_t>(std::max(1u, std::min(hw, 16u)),
+                                             std::max<size_t>(1, bytes / min_chunk));
+    if (nt <= 1) {
+        memcpy(dst, src, bytes);
+        return;
+    }
+    std::vector<std::thread> th;
+    size_t per = (bytes + nt - 1) / nt;
+    per = (per + 63) & ~size_t(63);
+    for (unsigned t = 0; t < nt; ++t) {
+        size_t off = per * t;
+        if (off >= bytes) break;
+        size_t n = std::min(per, bytes - off);
+        th.emplace_back([=] { memcpy((char*)dst + off, (const char*)src + off, n); });
+    }
+    for (auto& x : th) x.join();
+}
+
+int fill_params(ebsd_handle* h, const ebsd_epilogue* e, FwdParams& p)
+{
+    memset(&p, 0, sizeof p);
+    p.master = h->d_master_il;
+    p.rg = h->d_rg;
+    p.W = h->d_W;
+    p.numsx = h->geom.numsx;
+    p.numsy = h->geom.numsy;
+    p.P = h->P;
+    p.npx = h->npx;
+    p.npy = h->npy;
+    p.gx = 2 * h->npx + 1;
+    p.scl = host::lambert_scale(h->npx);
+    p.spi2 = host::lambert_spi2_f();
+    if (e) {
+        if (e->scalingmode < EBSD_SCALING_NOT || e->scalingmode > EBSD_SCALING_GAM)
+            return set_err(h, EBSD_EINVAL, "scalingmode %d is not 0 ('not'), 1 ('lin') or 2 ('gam')",
+                           e->scalingmode);
+        const int b = e->binning;
+        if (b != 1 && b != 2 && b != 4 && b != 8)
+            return set_err(h, EBSD_EUNSUPPORTED, "binning %d: supported values are 1, 2, 4, 8", b);
+        p.prefactor = e->prefactor;
+        p.binning = b;
+        p.mode = e->scalingmode;
+        p.gammavalue = e->gammavalue;
+        const float fb = (float)b;
+        p.bindx = 1.0f / (fb * fb);
+        p.poisson = e->poisson;
+        p.seed = e->seed;
+        if (p.mode == EBSD_SCALING_NOT || b == 1) {
+            p.out_nx = p.numsx;
+            p.out_ny = p.numsy;
+        } else {
+            p.out_nx = p.numsx / b;
+            p.out_ny = p.numsy / b;
+            if (p.out_nx < 1 || p.out_ny < 1)
+                return set_err(h, EBSD_EINVAL, "binning %d leaves no full block on a %dx%d detector",
+                               b, p.numsx, p.numsy);
+        }
+        if (e->poisson)
+            return set_err(h, EBSD_EUNSUPPORTED, "Poisson noise is not available in this build");
+    }
+    return EBSD_OK;
+}
+
+int check_ready(ebsd_handle* h)
+{
+    if (!h) return set_err(nullptr, EBSD_EINVAL, "null handle");
+    if (!h->have_master) return set_err(h, EBSD_ESTATE, "no master pattern: call ebsd_set_master first");
+    if (!h->have_detector)
+        return set_err(h, EBSD_ESTATE, "no detector: call ebsd_set_detector first");
+    return EBSD_OK;
+}
+
+int check_quats_host(ebsd_handle* h, const float* q, int64_t n)
+{
+    for (int64_t i = 0; i < 4 * n; ++i)
+        if (!std::isfinite(q[i]))
+            return set_err(h, EBSD_EINVAL, "quaternion %lld has a non-finite component",
+                           (long long)(i / 4));
+    return EBSD_OK;
+}
+
+int launch_chunk(ebsd_handle* h, FwdParams p, const float4* dq, int64_t n, float* dout)
+{
+    p.quats = dq;
+    p.n = n;
+    p.out = dout;
+    cudaError_t e = launch_forward(p, h->NV, h->cfg, h->stream);
+    if (e != cudaSuccess) return cuda_err(h, e, "forward kernel launch");
+    return EBSD_OK;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------
+
+extern "C" int ebsd_version(void) { return 100; }
+
+extern "C" int ebsd_create(ebsd_handle** out, int device)
+{
+    if (!out) return set_err(nullptr, EBSD_EINVAL, "ebsd_create: null output pointer");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(nullptr, EBSD_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= ndev)
+        return set_err(nullptr, EBSD_EINVAL, "device %d out of range (%d devices)", device, ndev);
+    ebsd_handle* h = new ebsd_handle();
+    h->device = device;
+    e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaEventCreateWithFlags(&h->ev_comp[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_d2h[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        int rc = set_err(nullptr, EBSD_ECUDA, "ebsd_create: %s", cudaGetErrorString(e));
+        ebsd_destroy(h);
+        return rc;
+    }
+    h->stream = h->own_stream;
+    cudaDeviceGetAttribute(&h->max_persist, cudaDevAttrMaxPersistingL2CacheSize, device);
+    cudaDeviceGetAttribute(&h->max_window, cudaDevAttrMaxAccessPolicyWindowSize, device);
+    cudaGetLastError();
+    *out = h;
+    return EBSD_OK;
+}
+
+extern "C" void ebsd_destroy(ebsd_handle* h)
+{
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+    cudaFree(h->d_master_raw);
+    cudaFree(h->d_master_il);
+    cudaFree(h->d_rg);
+    cudaFree(h->d_W);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(h->quats[i].ptr);
+        cudaFree(h->outb[i].ptr);
+        if (h->pinned[i]) cudaFreeHost(h->pinned[i]);
+        if (h->ev_comp[i]) cudaEventDestroy(h->ev_comp[i]);
+        if (h->ev_d2h[i]) cudaEventDestroy(h->ev_d2h[i]);
+    }
+    cudaFree(h->tmp.ptr);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    cudaGetLastError();
+    delete h;
+}
+
+extern "C" const char* ebsd_last_error(const ebsd_handle* h)
+{
+    return h ? h->err.c_str() : g_err.c_str();
+}
+
+extern "C" int ebsd_set_stream(ebsd_handle* h, void* stream)
+{
+    if (!h) return set_err(nullptr, EBSD_EINVAL, "null handle");
+    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
+{
+    if (!h) return set_err(nullptr, EBSD_EINVAL, "null handle");
+    if (!key) return set_err(h, EBSD_EINVAL, "ebsd_set_option: null key");
+    const std::string k(key);
+    if (k == "weights_fp64") {
+        h->weights_fp64 = value != 0;
+        if (h->have_detector)
+            return set_err(h, EBSD_ESTATE, "weights_fp64 applies at the next ebsd_set_detector");
+    } else if (k == "tile_y") {
+        if (value != 4 && value != 8 && value != 16)
+            return set_err(h, EBSD_EINVAL, "tile_y must be 4, 8 or 16");
+        h->cfg.tile_y = (int)value;
+    } else if (k == "orient_per_cta") {
+        if (value < 1 || value > 64)
+            return set_err(h, EBSD_EINVAL, "orient_per_cta must be in 1..64");
+        h->cfg.orient_per_cta = (int)value;
+    } else {
+        return set_err(h, EBSD_EINVAL, "unknown option '%s'", key);
+    }
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_set_master(ebsd_handle* h, const float* sr, int32_t npx, int32_t npy,
+                               int32_t nE, int32_t numset)
+{
+    if (!h) return set_err(nullptr, EBSD_EINVAL, "null handle");
+    if (!sr) return set_err(h, EBSD_EINVAL, "ebsd_set_master: null sr");
+    if (npx < 1 || npy < 1 || nE < 1 || numset < 1)
+        return set_err(h, EBSD_EINVAL, "ebsd_set_master: npx=%d npy=%d nE=%d numset=%d must be >= 1",
+                       npx, npy, nE, numset);
+    if (nE > 4 * kMaxNV)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_set_master: nE=%d exceeds %d energy bins", nE,
+                       4 * kMaxNV);
+    int rc = activate(h);
+    if (rc) return rc;
+    const size_t n = (size_t)(2 * npx + 1) * (2 * npy + 1) * nE * numset;
+    cudaStreamSynchronize(h->stream);
+    cudaFree(h->d_master_raw);
+    h->d_master_raw = nullptr;
+    h->have_master = false;
+    h->il_e0 = -1;
+    CK(h, cudaMalloc(&h->d_master_raw, n * sizeof(float)), "cudaMalloc master");
+    CK(h, cudaMemcpy(h->d_master_raw, sr, n * sizeof(float), cudaMemcpyHostToDevice),
+       "master upload");
+    h->npx = npx;
+    h->npy = npy;
+    h->nE = nE;
+    h->numset = numset;
+    // maxval(sr) of the set sum, printed by the program (CTEMEBSD.f90:548)
+    float mx = -INFINITY;
+    const size_t plane = (size_t)(2 * npx + 1) * (2 * npy + 1) * nE;
+    for (size_t i = 0; i < plane; ++i) {
+        float s = 0.0f;
+        for (int st = 0; st < numset; ++st) s = s + sr[i + plane * st];
+        mx = std::max(mx, s);
+    }
+    h->max_sr = mx;
+    h->have_master = true;
+    if (h->have_detector) h->have_detector = false;  // window must be rebuilt
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_energy_window(float energymin, float energymax, double Ehistmin,
+                                  double Ebinsize, int32_t numEbins, int32_t* Emin, int32_t* Emax)
+{
+    if (!Emin || !Emax || numEbins < 1 || !(Ebinsize != 0.0))
+        return set_err(nullptr, EBSD_EINVAL, "ebsd_energy_window: invalid arguments");
+    host::energy_window(energymin, energymax, Ehistmin, Ebinsize, numEbins, Emin, Emax);
+    return EBSD_OK;
+}
+
+extern "C" double ebsd_prefactor(double beamcurrent, double dwelltime, int32_t num_el)
+{
+    return host::prefactor(beamcurrent, dwelltime, num_el);
+}
+
+extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const int32_t* accum_e,
+                                 int32_t nsx, int32_t nsy, int32_t numEbins, int32_t Emin,
+                                 int32_t Emax, int32_t* num_el)
+{
+    if (!h) return set_err(nullptr, EBSD_EINVAL, "null handle");
+    if (!g || !accum_e) return set_err(h, EBSD_EINVAL, "ebsd_set_detector: null argument");
+    if (!h->have_master)
+        return set_err(h, EBSD_ESTATE, "ebsd_set_detector: set the master pattern first");
+    if (numEbins != h->nE)
+        return set_err(h, EBSD_EINVAL,
+                       "Energy histogram and Lambert stack have different energy dimension "
+                       "(MC numEbins=%d, master nE=%d)",
+                       numEbins, h->nE);
+    if (g->numsx < 1 || g->numsy < 1 || (int64_t)g->numsx * g->numsy > (1LL << 30))
+        return set_err(h, EBSD_EINVAL, "detector %dx%d out of range", g->numsx, g->numsy);
+    if (nsx < 1 || nsy < 1) return set_err(h, EBSD_EINVAL, "MC grid nsx=%d nsy=%d", nsx, nsy);
+    if (Emin < 1 || Emax > numEbins || Emin > Emax)
+        return set_err(h, EBSD_EINVAL, "energy window %d..%d outside 1..%d", Emin, Emax, numEbins);
+    if (!(g->L > 0.0f) || !std::isfinite(g->delta) || !std::isfinite(g->xpc) ||
+        !std::isfinite(g->ypc) || !std::isfinite(g->thetac) || !std::isfinite(g->sig))
+        return set_err(h, EBSD_EINVAL, "detector geometry has a non-finite or non-positive value");
+    int rc = activate(h);
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    cudaStreamSynchronize(s);
+    h->have_detector = false;
+
+    const int P = g->numsx * g->numsy;
+    const int nsel = Emax - Emin + 1;
+    const int NV = (nsel + 3) / 4;
+    cudaFree(h->d_rg);
+    cudaFree(h->d_W);
+    h->d_rg = nullptr;
+    h->d_W = nullptr;
+    CK(h, cudaMalloc(&h->d_rg, sizeof(float4) * (size_t)P), "cudaMalloc rg");
+    CK(h, cudaMalloc(&h->d_W, sizeof(float4) * (size_t)P * NV), "cudaMalloc W");
+
+    // master re-layout for this window
+    if (h->il_e0 != Emin - 1 || h->il_nsel != nsel) {
+        cudaFree(h->d_master_il);
+        h->d_master_il = nullptr;
+        h->il_bytes = sizeof(float4) * (size_t)(2 * h->npx + 1) * (2 * h->npy + 1) * NV;
+        CK(h, cudaMalloc(&h->d_master_il, h->il_bytes), "cudaMalloc master layout");
+        CK(h, launch_master_relayout(h->d_master_raw, h->npx, h->npy, h->nE, h->numset, Emin - 1,
+                                     nsel, NV, h->d_master_il, s),
+           "master re-layout");
+        h->il_e0 = Emin - 1;
+        h->il_nsel = nsel;
+    }
+
+    float ca, sa;
+    host::detector_angles(g->sig, g->thetac, &ca, &sa);
+    CK(h, launch_detector(*g, ca, sa, h->d_rg, s), "detector kernel");
+
+    const size_t acc_bytes = sizeof(int32_t) * (size_t)numEbins * (2 * nsx + 1) * (2 * nsy + 1);
+    rc = ensure(h, h->tmp, std::max(acc_bytes, sizeof(float) * 4), "MC histogram");
+    if (rc) return rc;
+    CK(h, cudaMemcpyAsync(h->tmp.ptr, accum_e, acc_bytes, cudaMemcpyHostToDevice, s),
+       "MC upload");
+    const float sclmc = host::lambert_scale(nsx);
+    float4* d_wref = nullptr;
+    CK(h, cudaMalloc(&d_wref, sizeof(float4) * (size_t)P * NV), "cudaMalloc weights");
+    cudaError_t e = launch_weights(h->d_rg, P, (const int32_t*)h->tmp.ptr, numEbins, nsx, nsy,
+                                   sclmc, host::lambert_spi2_f(), Emin - 1, nsel, NV,
+                                   h->weights_fp64, *g, h->d_W, d_wref, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // num_el reuses the start of the histogram buffer, after the weights ran
+    float* d_sum = (float*)h->tmp.ptr;
+    if (e == cudaSuccess) e = launch_num_el(d_wref, P, nsel, NV, d_sum, s);
+    float sum = 0.0f;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&sum, d_sum, sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_wref);
+    if (e != cudaSuccess) return cuda_err(h, e, "detector weights");
+    h->num_el = (int32_t)lroundf(sum);
+    if (num_el) *num_el = h->num_el;
+
+    h->geom = *g;
+    h->Emin = Emin;
+    h->Emax = Emax;
+    h->nsel = nsel;
+    h->NV = NV;
+    h->P = P;
+
+    // keep the master resident in L2 for the pattern kernels
+    if (h->max_persist > 0) {
+        size_t want = std::min(h->il_bytes, (size_t)h->max_persist);
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want);
+        cudaGetLastError();
+    }
+    h->have_detector = true;
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_output_dims(const ebsd_handle* hc, const ebsd_epilogue* e, int32_t* nx,
+                                int32_t* ny)
+{
+    ebsd_handle* h = const_cast<ebsd_handle*>(hc);
+    int rc = check_ready(h);
+    if (rc) return rc;
+    FwdParams p;
+    rc = fill_params(h, e, p);
+    if (rc) return rc;
+    if (nx) *nx = p.out_nx;
+    if (ny) *ny = p.out_ny;
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
+                            float* out)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n < 0) return set_err(h, EBSD_EINVAL, "negative orientation count");
+    if (n == 0) return EBSD_OK;
+    if (!quats || !out || !e) return set_err(h, EBSD_EINVAL, "ebsd_forward: null argument");
+    rc = activate(h);
+    if (rc) return rc;
+    FwdParams p;
+    rc = fill_params(h, e, p);
+    if (rc) return rc;
+    const size_t rec = (size_t)p.out_nx * p.out_ny;
+    const PtrKind qk = ptr_kind(quats), ok = ptr_kind(out);
+    if (qk != kDevice) {
+        rc = check_quats_host(h, quats, n);
+        if (rc) return rc;
+    }
+    cudaStream_t s = h->stream;
+
+    if (ok == kDevice) {
+        const float4* dq = (const float4*)quats;
+        if (qk != kDevice) {
+            rc = ensure(h, h->quats[0], sizeof(float4) * (size_t)n, "quaternions");
+            if (rc) return rc;
+            CK(h, cudaMemcpyAsync(h->quats[0].ptr, quats, sizeof(float4) * n,
+                                  cudaMemcpyHostToDevice, s),
+               "quaternion upload");
+            dq = (const float4*)h->quats[0].ptr;
+        }
+        return launch_chunk(h, p, dq, n, out);
+    }
+
+    // Host output: chunks of orientations, computed on the work stream and
+    // copied back on the copy stream, double-buffered.
+    const size_t budget = size_t(256) << 20;
+    int64_t chunk = (int64_t)std::max<size_t>(1, budget / (rec * sizeof(float)));
+    chunk = std::min<int64_t>(chunk, n);
+    const size_t cbytes = (size_t)chunk * rec * sizeof(float);
+    for (int b = 0; b < 2; ++b) {
+        rc = ensure(h, h->outb[b], cbytes, "pattern chunk");
+        if (rc) return rc;
+        if (qk != kDevice) {
+            rc = ensure(h, h->quats[b], sizeof(float4) * (size_t)chunk, "quaternions");
+            if (rc) return rc;
+        }
+    }
+    const bool stage = ok == kPageable;
+    if (stage && h->pinned_bytes < cbytes) {
+        for (int b = 0; b < 2; ++b) {
+            if (h->pinned[b]) cudaFreeHost(h->pinned[b]);
+            h->pinned[b] = nullptr;
+        }
+        h->pinned_bytes = 0;
+        for (int b = 0; b < 2; ++b) CK(h, cudaMallocHost(&h->pinned[b], cbytes), "pinned staging");
+        h->pinned_bytes = cbytes;
+    }
+    const int64_t nchunks = (n + chunk - 1) / chunk;
+    // fresh events for this call's ordering
+    for (int b = 0; b < 2; ++b) CK(h, cudaEventRecord(h->ev_d2h[b], h->copy_stream), "event");
+    auto finish = [&](int64_t c) -> int {
+        const int b = (int)(c & 1);
+        CK(h, cudaEventSynchronize(h->ev_d2h[b]), "pattern copy");
+        if (stage) {
+            const int64_t o0 = c * chunk;
+            const int64_t m = std::min<int64_t>(chunk, n - o0);
+            parallel_memcpy(out + (size_t)o0 * rec, h->pinned[b], (size_t)m * rec * sizeof(float));
+        }
+        return EBSD_OK;
+    };
+    for (int64_t c = 0; c < nchunks; ++c) {
+        const int b = (int)(c & 1);
+        const int64_t o0 = c * chunk;
+        const int64_t m = std::min<int64_t>(chunk, n - o0);
+        if (stage && c >= 2) {
+            rc = finish(c - 2);  // staging buffer b must be drained first
+            if (rc) return rc;
+        }
+        CK(h, cudaStreamWaitEvent(s, h->ev_d2h[b], 0), "wait");
+        const float4* dq;
+        if (qk == kDevice) {
+            dq = (const float4*)quats + o0;
+        } else {
+            CK(h, cudaMemcpyAsync(h->quats[b].ptr, quats + 4 * o0, sizeof(float4) * m,
+                                  cudaMemcpyHostToDevice, s),
+               "quaternion upload");
+            dq = (const float4*)h->quats[b].ptr;
+        }
+        rc = launch_chunk(h, p, dq, m, (float*)h->outb[b].ptr);
+        if (rc) return rc;
+        CK(h, cudaEventRecord(h->ev_comp[b], s), "event");
+        CK(h, cudaStreamWaitEvent(h->copy_stream, h->ev_comp[b], 0), "wait");
+        float* dst = stage ? h->pinned[b] : out + (size_t)o0 * rec;
+        CK(h, cudaMemcpyAsync(dst, h->outb[b].ptr, (size_t)m * rec * sizeof(float),
+                              cudaMemcpyDeviceToHost, h->copy_stream),
+           "pattern copy");
+        CK(h, cudaEventRecord(h->ev_d2h[b], h->copy_stream), "event");
+    }
+    if (stage) {
+        for (int64_t c = std::max<int64_t>(0, nchunks - 2); c < nchunks; ++c) {
+            rc = finish(c);
+            if (rc) return rc;
+        }
+    } else {
+        CK(h, cudaStreamSynchronize(h->copy_stream), "pattern copy");
+    }
+    // the caller's stream sees completed work
+    CK(h, cudaStreamSynchronize(s), "forward");
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_cells(ebsd_handle* h, const float* quats, int64_t n, int32_t* nix,
+                          int32_t* niy, float* ixy0, float* ixy1)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n < 0 || !quats || !nix || !niy || !ixy0 || !ixy1)
+        return set_err(h, EBSD_EINVAL, "ebsd_cells: invalid arguments");
+    if (n == 0) return EBSD_OK;
+    rc = activate(h);
+    if (rc) return rc;
+    FwdParams p;
+    rc = fill_params(h, nullptr, p);
+    if (rc) return rc;
+    const size_t total = (size_t)n * h->P;
+    const bool dev = ptr_kind(nix) == kDevice;
+    cudaStream_t s = h->stream;
+    DeviceBuf qb, ob;
+    const float4* dq = (const float4*)quats;
+    if (ptr_kind(quats) != kDevice) {
+        rc = ensure(h, qb, sizeof(float4) * n, "quaternions");
+        if (rc) return rc;
+        CK(h, cudaMemcpyAsync(qb.ptr, quats, sizeof(float4) * n, cudaMemcpyHostToDevice, s), "upload");
+        dq = (const float4*)qb.ptr;
+    }
+    p.quats = dq;
+    p.n = n;
+    if (dev) {
+        p.nix = nix;
+        p.niy = niy;
+        p.ixy0 = ixy0;
+        p.ixy1 = ixy1;
+    } else {
+        rc = ensure(h, ob, total * 16, "cells");
+        if (rc) {
+            cudaFree(qb.ptr);
+            return rc;
+        }
+        char* base = (char*)ob.ptr;
+        p.nix = (int32_t*)base;
+        p.niy = (int32_t*)(base + total * 4);
+        p.ixy0 = (float*)(base + total * 8);
+        p.ixy1 = (float*)(base + total * 12);
+    }
+    cudaError_t e = launch_cells(p, h->NV, s);
+    if (e == cudaSuccess && !dev) {
+        e = cudaMemcpyAsync(nix, p.nix, total * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(niy, p.niy, total * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ixy0, p.ixy0, total * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ixy1, p.ixy1, total * 4, cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(qb.ptr);
+    cudaFree(ob.ptr);
+    if (e != cudaSuccess) return cuda_err(h, e, "ebsd_cells");
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_get_detector(ebsd_handle* h, float* W, float* rgx, float* rgy, float* rgz)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    rc = activate(h);
+    if (rc) return rc;
+    const int P = h->P;
+    CK(h, cudaStreamSynchronize(h->stream), "sync");
+    if (rgx || rgy || rgz) {
+        std::vector<float4> rg(P);
+        CK(h, cudaMemcpy(rg.data(), h->d_rg, sizeof(float4) * P, cudaMemcpyDeviceToHost), "rg");
+        for (int i = 0; i < P; ++i) {
+            if (rgx) rgx[i] = rg[i].x;
+            if (rgy) rgy[i] = rg[i].y;
+            if (rgz) rgz[i] = rg[i].z;
+        }
+    }
+    if (W) {
+        std::vector<float4> w((size_t)P * h->NV);
+        CK(h, cudaMemcpy(w.data(), h->d_W, sizeof(float4) * w.size(), cudaMemcpyDeviceToHost), "W");
+        const int nE = h->nE;
+        memset(W, 0, sizeof(float) * (size_t)nE * P);
+        const float* wf = (const float*)w.data();
+        for (int p = 0; p < P; ++p)
+            for (int k = 0; k < h->nsel; ++k) {
+                const int c = k / 4, t = k % 4;
+                W[(size_t)p * nE + (h->Emin - 1 + k)] = wf[((size_t)c * P + p) * 4 + t];
+            }
+    }
+    return EBSD_OK;
+}
+
+// Internal accessors for the program driver (ebsd_program.cpp).
+namespace ebsd {
+namespace host {
+float handle_max_sr(const ebsd_handle* h) { return h->max_sr; }
+int handle_set_error(ebsd_handle* h, int code, const char* msg)
+{
+    return set_err(h, code, "%s", msg);
+}
+int global_set_error(int code, const char* msg) { return set_err(nullptr, code, "%s", msg); }
+}  // namespace host
+}  // namespace ebsd

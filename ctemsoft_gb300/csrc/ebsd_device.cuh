@@ -1,0 +1,83 @@
+// Device-side arithmetic of the EBSD pattern loop.
+//
+// Every translation unit that includes this file is compiled with
+// -fmad=false and IEEE division/square root, so each float expression below
+// is one correctly rounded binary32 operation per operator, evaluated left
+// to right exactly as gfortran evaluates the cited Fortran.  Where a fused
+// multiply-add is wanted it is written as fmaf() explicitly.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ebsd {
+
+// qq3 = q (x) (0,r) (x) conjg(q), quaternions.f90:255-264,306-313 as used at
+// CTEMEBSD.f90:577-586; returns the vector part.
+__device__ __forceinline__ void rotate_direction(const float4 q, float rx, float ry, float rz,
+                                                 float& d0, float& d1, float& d2)
+{
+    const float x0 = 0.0f;
+    const float y0 = q.x, y1 = -q.y, y2 = -q.z, y3 = -q.w;   // conjg(q)
+    const float t0 = x0 * y0 - rx * y1 - ry * y2 - rz * y3;   // quat_mult(qq, qq1)
+    const float t1 = x0 * y1 + rx * y0 + ry * y3 - rz * y2;
+    const float t2 = x0 * y2 - rx * y3 + ry * y0 + rz * y1;
+    const float t3 = x0 * y3 + rx * y2 - ry * y1 + rz * y0;
+    d0 = q.x * t1 + q.y * t0 + q.z * t3 - q.w * t2;           // quat_mult(qq2, t)
+    d1 = q.x * t2 - q.y * t3 + q.z * t0 + q.w * t1;
+    d2 = q.x * t3 + q.y * t2 - q.z * t1 + q.w * t0;
+}
+
+// dc = dc/sqrt(sum(dc**2)); if (dc(3) < 0) dc = -dc   (CTEMEBSD.f90:588-589)
+__device__ __forceinline__ void normalize_fold(float& d0, float& d1, float& d2)
+{
+    float s = d0 * d0;
+    s = s + d1 * d1;
+    s = s + d2 * d2;
+    s = sqrtf(s);
+    d0 = d0 / s;
+    d1 = d1 / s;
+    d2 = d2 / s;
+    if (d2 < 0.0f) {
+        d0 = -d0;
+        d1 = -d1;
+        d2 = -d2;
+    }
+}
+
+// Lambert2DSquareInverseSingle, Lambert.f90:405-436.  spi2 = sngl(LPs%sPi2).
+// abs(x)/x * sqrt(.) is +-sqrt(.) exactly for x != 0, and x == 0 only
+// reaches this branch together with y == 0, which |z| == 1 intercepts.
+__device__ __forceinline__ void lambert_inverse(float x, float y, float z, float spi2,
+                                                float& X, float& Y)
+{
+    float s = x * x;
+    s = s + y * y;
+    s = s + z * z;
+    if (fabsf(1.0f - s) > 1.0e-6f || fabsf(z) == 1.0f) {
+        X = 0.0f;
+        Y = 0.0f;
+    } else if (fabsf(y) <= fabsf(x)) {
+        const float q = copysignf(sqrtf(2.0f * (1.0f - z)), x);
+        X = q * spi2;
+        Y = q * atanf(y / x) / spi2;
+    } else {
+        const float q = copysignf(sqrtf(2.0f * (1.0f - z)), y);
+        X = q * atanf(x / y) / spi2;
+        Y = q * spi2;
+    }
+}
+
+// Cell index and bilinear fractions, CTEMEBSD.f90:593-598:
+// nix = int(npx + ixy) - npx (float add, then truncation), dx = ixy - nix.
+// Returns the 0-based grid column of the lower corner, clamped to the grid.
+__device__ __forceinline__ int lambert_cell(float ixy, int np, float& d, int& ni)
+{
+    ni = __float2int_rz((float)np + ixy) - np;
+    d = ixy - (float)ni;
+    int i0 = ni + np;
+    i0 = i0 < 0 ? 0 : (i0 > 2 * np ? 2 * np : i0);
+    return i0;
+}
+
+}  // namespace ebsd

@@ -1,0 +1,204 @@
+// The EBSD pattern loop on sm_103a: CTEMEBSD.f90:573-658.
+//
+// One CTA covers a 32 x tile_y block of detector pixels (one warp per
+// detector row segment, so pattern stores are 128-byte coalesced) for a run
+// of orientations.  Each thread loads its pixel's direction cosine and its
+// NV float4 vectors of energy weights once and reuses them for every
+// orientation of the run.  Per orientation it rotates the direction,
+// projects it with the square Lambert map, and gathers the four master
+// nodes around it: the master is stored energy-fastest (NV float4 per
+// node), so one corner's bins arrive in NV 128-bit read-only loads that hit
+// the L2-resident (persisting) master.
+//
+// Arithmetic follows the reference operation by operation (the TU is
+// compiled with -fmad=false, IEEE div/sqrt): the summation order of :600-604,
+// the binary64 prefactor multiply of :608, the column-major block sums of
+// :636 and powf for 'gam'.  Only atanf and powf are CUDA's own.
+#include "ebsd_device.cuh"
+#include "ebsd_internal.h"
+
+namespace ebsd {
+
+namespace {
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Sum over the window of W(k) * bilinear(sr(.,.,k)), the loop body of
+// CTEMEBSD.f90:600-604 in its own evaluation order.
+template <int NV>
+__device__ __forceinline__ float gather_pixel(const float4* __restrict__ master, int gx,
+                                              int ix0, int iy0, int ix1, int iy1, float dx,
+                                              float dy, const float4 (&w)[NV])
+{
+    const float dxm = 1.0f - dx, dym = 1.0f - dy;
+    const float4* m00 = master + ((int64_t)iy0 * gx + ix0) * NV;
+    const float4* m10 = master + ((int64_t)iy0 * gx + ix1) * NV;
+    const float4* m01 = master + ((int64_t)iy1 * gx + ix0) * NV;
+    const float4* m11 = master + ((int64_t)iy1 * gx + ix1) * NV;
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        const float4 a = ldg4(m00 + c), b = ldg4(m10 + c), e = ldg4(m01 + c), f = ldg4(m11 + c);
+        acc = acc + w[c].x * (a.x * dxm * dym + b.x * dx * dym + e.x * dxm * dy + f.x * dx * dy);
+        acc = acc + w[c].y * (a.y * dxm * dym + b.y * dx * dym + e.y * dxm * dy + f.y * dx * dy);
+        acc = acc + w[c].z * (a.z * dxm * dym + b.z * dx * dym + e.z * dxm * dy + f.z * dx * dy);
+        acc = acc + w[c].w * (a.w * dxm * dym + b.w * dx * dym + e.w * dxm * dy + f.w * dx * dy);
+    }
+    return acc;
+}
+
+// Rotated, projected and scaled Lambert coordinates of one pixel for one
+// orientation (CTEMEBSD.f90:584-591).
+__device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, float scl,
+                                              float spi2, float& ixy0, float& ixy1)
+{
+    float d0, d1, d2;
+    rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
+    normalize_fold(d0, d1, d2);
+    float X, Y;
+    lambert_inverse(d0, d1, d2, spi2, X, Y);
+    ixy0 = scl * X;
+    ixy1 = scl * Y;
+}
+
+template <int NV>
+__global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y, int tiles_x,
+                                                 int ntiles, int opc)
+{
+    extern __shared__ float tile[];  // [tile_y][33], binning only
+    const int tid = threadIdx.x;
+    const int tx = tid & 31, ty = tid >> 5;
+    const int t = (int)(blockIdx.x % (unsigned)ntiles);
+    const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
+    const int x = (t % tiles_x) * kTileX + tx;
+    const int y = (t / tiles_x) * tile_y + ty;
+    const bool inside = x < prm.numsx && y < prm.numsy;
+    const int p = y * prm.numsx + x;
+
+    float4 r = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+    float4 w[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) w[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (inside) {
+        r = prm.rg[p];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) w[c] = prm.W[(int64_t)c * prm.P + p];
+    }
+    const bool binned = prm.mode != EBSD_SCALING_NOT && prm.binning > 1;
+    const int64_t rec = (int64_t)prm.out_nx * prm.out_ny;
+
+    int64_t o_end = o_begin + opc;
+    if (o_end > prm.n) o_end = prm.n;
+    for (int64_t o = o_begin; o < o_end; ++o) {
+        float val = 0.0f;
+        if (inside) {
+            const float4 q = ldg4(prm.quats + o);
+            float ixy0, ixy1;
+            pixel_lambert(q, r, prm.scl, prm.spi2, ixy0, ixy1);
+            float dx, dy;
+            int nix, niy;
+            const int ix0 = lambert_cell(ixy0, prm.npx, dx, nix);
+            const int iy0 = lambert_cell(ixy1, prm.npy, dy, niy);
+            const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
+            const float acc = gather_pixel<NV>(prm.master, prm.gx, ix0, iy0, ix1, iy1, dx, dy, w);
+            val = (float)(prm.prefactor * (double)acc);                      // :608
+        }
+        if (!binned) {
+            if (prm.mode == EBSD_SCALING_GAM) val = powf(val, prm.gammavalue);  // :647-649
+            if (inside) __stcs(prm.out + o * rec + p, val);
+        } else {
+            const int b = prm.binning;
+            tile[ty * 33 + tx] = val;
+            __syncthreads();
+            const int nbx = kTileX / b, nby = tile_y / b;
+            if (tx < nbx && ty < nby) {
+                float s = 0.0f;                                              // :636 sum()
+                for (int jj = 0; jj < b; ++jj)
+                    for (int ii = 0; ii < b; ++ii) s = s + tile[(ty * b + jj) * 33 + tx * b + ii];
+                s = s * prm.bindx;                                           // :640
+                if (prm.mode == EBSD_SCALING_GAM) s = powf(s, prm.gammavalue);
+                const int X = ((t % tiles_x) * kTileX) / b + tx;
+                const int Y = ((t / tiles_x) * tile_y) / b + ty;
+                if (X < prm.out_nx && Y < prm.out_ny)
+                    __stcs(prm.out + o * rec + (int64_t)Y * prm.out_nx + X, s);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Cell diagnostics: nix/niy/ixy per pixel and orientation.
+__global__ void k_cells(const FwdParams prm)
+{
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = prm.n * prm.P;
+    if (idx >= total) return;
+    const int64_t o = idx / prm.P;
+    const int p = (int)(idx - o * prm.P);
+    float ixy0, ixy1;
+    pixel_lambert(prm.quats[o], prm.rg[p], prm.scl, prm.spi2, ixy0, ixy1);
+    float dx, dy;
+    int nix, niy;
+    lambert_cell(ixy0, prm.npx, dx, nix);
+    lambert_cell(ixy1, prm.npy, dy, niy);
+    prm.nix[idx] = nix;
+    prm.niy[idx] = niy;
+    prm.ixy0[idx] = ixy0;
+    prm.ixy1[idx] = ixy1;
+}
+
+template <int NV>
+cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
+{
+    const int tile_y = cfg.tile_y;
+    const int tiles_x = (p.numsx + kTileX - 1) / kTileX;
+    const int tiles_y = (p.numsy + tile_y - 1) / tile_y;
+    const int ntiles = tiles_x * tiles_y;
+    const int opc = cfg.orient_per_cta;
+    const int64_t oblocks = (p.n + opc - 1) / opc;
+    const int64_t blocks = oblocks * ntiles;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const size_t smem = sizeof(float) * 33 * tile_y;
+    k_forward<NV><<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, tile_y, tiles_x, ntiles,
+                                                                   opc);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s)
+{
+    if (p.n <= 0) return cudaSuccess;
+    switch (NV) {
+        case 1: return launch_nv<1>(p, cfg, s);
+        case 2: return launch_nv<2>(p, cfg, s);
+        case 3: return launch_nv<3>(p, cfg, s);
+        case 4: return launch_nv<4>(p, cfg, s);
+        case 5: return launch_nv<5>(p, cfg, s);
+        case 6: return launch_nv<6>(p, cfg, s);
+        case 7: return launch_nv<7>(p, cfg, s);
+        case 8: return launch_nv<8>(p, cfg, s);
+        case 9: return launch_nv<9>(p, cfg, s);
+        case 10: return launch_nv<10>(p, cfg, s);
+        case 11: return launch_nv<11>(p, cfg, s);
+        case 12: return launch_nv<12>(p, cfg, s);
+        case 13: return launch_nv<13>(p, cfg, s);
+        case 14: return launch_nv<14>(p, cfg, s);
+        case 15: return launch_nv<15>(p, cfg, s);
+        case 16: return launch_nv<16>(p, cfg, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_cells(const FwdParams& p, int /*NV*/, cudaStream_t s)
+{
+    const int64_t total = p.n * p.P;
+    if (total <= 0) return cudaSuccess;
+    const int bs = 256;
+    const int64_t blocks = (total + bs - 1) / bs;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    k_cells<<<(unsigned)blocks, bs, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace ebsd

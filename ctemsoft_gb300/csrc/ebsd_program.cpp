@@ -1,0 +1,193 @@
+// The CTEMEBSD program on the GPU: CTEMEBSD.f90:87-672 end to end, with the
+// pattern loop replaced by libebsdgpu calls and the output written by a
+// writer thread while the next chunk of patterns is computed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ebsd_host.h"
+
+using namespace ebsd;
+
+namespace {
+
+struct HandleGuard {
+    ebsd_handle* h = nullptr;
+    ~HandleGuard() { ebsd_destroy(h); }
+};
+
+struct PinnedGuard {
+    float* p[2] = {nullptr, nullptr};
+    ~PinnedGuard()
+    {
+        for (auto q : p)
+            if (q) cudaFreeHost(q);
+    }
+};
+
+int fail(int code, const std::string& msg)
+{
+    host::global_set_error(code, msg.c_str());
+    return code;
+}
+
+}  // namespace
+
+extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
+{
+    auto say = [&](const char* fmt, auto... args) {
+        if (!quiet) {
+            printf(fmt, args...);
+            fflush(stdout);
+        }
+    };
+    say(" CTEMEBSD (GB300): Dynamical EBSD patterns, using precomputed MC and master Lambert "
+        "projections\n");
+
+    ebsd_namelist nml;
+    std::string err;
+    int rc = host::read_namelist(nmlfile, &nml, &err);
+    if (rc) return fail(rc, err);
+
+    // angle file (:228-288)
+    std::vector<float> quats;
+    rc = host::read_angle_file(nml.anglefile, nml.eulerconvention, nml.axisangle, &quats, &err);
+    if (rc) return fail(rc, err);
+    const int64_t numeuler = (int64_t)(quats.size() / 4);
+    say(" Number of angle entries = %lld\n", (long long)numeuler);
+
+    // MC file (:316-367)
+    say(" opening %s\n", nml.energyfile);
+    ebsd_mc_header mc;
+    std::vector<int32_t> accum_e;
+    rc = host::read_mc_file(nml.energyfile, &mc, &accum_e, nullptr, &err);
+    if (rc) return fail(rc, err);
+    say("  -> completed reading %s\n", nml.energyfile);
+    const int nsx = (mc.numsx - 1) / 2, nsy = (mc.numsy - 1) / 2;
+    int32_t Emin, Emax;
+    host::energy_window(nml.energymin, nml.energymax, mc.Ehistmin, mc.Ebinsize, mc.numEbins, &Emin,
+                        &Emax);
+    int64_t mcsum = 0;
+    for (int32_t v : accum_e) mcsum += v;
+    say(" shape(accum_e) = %d %d %d\n", mc.numEbins, 2 * nsx + 1, 2 * nsy + 1);
+    say(" energy range (Emin, Emax) = %d %d %lld\n", Emin, Emax, (long long)mcsum);
+
+    // master file (:378-406)
+    ebsd_master_header mh;
+    std::vector<float> srtmp;
+    rc = host::read_master_file(nml.FZfile, &mh, nullptr, nullptr, nullptr, &srtmp, &err);
+    if (rc) return fail(rc, err);
+    if (mh.nE != mc.numEbins) {
+        char buf[256];
+        snprintf(buf, sizeof buf,
+                 "Energy histogram and Lambert stack have different energy dimension; aborting "
+                 "program (histogram %d, Lambert stack %d)",
+                 mc.numEbins, mh.nE);
+        return fail(EBSD_EINVAL, buf);
+    }
+    say(" -> completed reading Master EBSD pattern file\n");
+
+    HandleGuard hg;
+    rc = ebsd_create(&hg.h, device);
+    if (rc) return rc;
+    ebsd_handle* h = hg.h;
+    auto herr = [&](int code) {
+        host::global_set_error(code, ebsd_last_error(h));
+        return code;
+    };
+    rc = ebsd_set_master(h, srtmp.data(), mh.npx, mh.npy, mh.nE, mh.numset);
+    if (rc) return herr(rc);
+    srtmp.clear();
+    srtmp.shrink_to_fit();
+
+    ebsd_geometry g;
+    g.L = nml.L;
+    g.thetac = nml.thetac;
+    g.delta = nml.delta;
+    g.numsx = nml.numsx;
+    g.numsy = nml.numsy;
+    g.xpc = nml.xpc;
+    g.ypc = nml.ypc;
+    g.sig = mc.sig;
+    int32_t num_el = 0;
+    rc = ebsd_set_detector(h, &g, accum_e.data(), nsx, nsy, mc.numEbins, Emin, Emax, &num_el);
+    if (rc) return herr(rc);
+    accum_e.clear();
+    accum_e.shrink_to_fit();
+
+    const double pref = host::prefactor(nml.beamcurrent, nml.dwelltime, num_el);
+    {
+        std::vector<float> W((size_t)mc.numEbins * g.numsx * g.numsy);
+        rc = ebsd_get_detector(h, W.data(), nullptr, nullptr, nullptr);
+        if (rc) return herr(rc);
+        float wmax = W.empty() ? 0.0f : *std::max_element(W.begin(), W.end());
+        say(" intensity prefactor = %.15g\n", pref);
+        say(" max accum_e_detector = %.8g\n", wmax);
+        say(" max sr = %.8g\n", host::handle_max_sr(h));
+    }
+
+    ebsd_epilogue epi;
+    memset(&epi, 0, sizeof epi);
+    epi.prefactor = pref;
+    epi.binning = nml.binning;
+    const std::string mode(nml.scalingmode);
+    epi.scalingmode = mode == "not" ? EBSD_SCALING_NOT
+                      : mode == "gam" ? EBSD_SCALING_GAM
+                                      : EBSD_SCALING_LIN;  // any other value bins (:630)
+    epi.gammavalue = nml.gammavalue;
+    epi.poisson = nml.poisson;
+    epi.seed = (uint64_t)nml.seed;
+    int32_t rx = 0, ry = 0;
+    rc = ebsd_output_dims(h, &epi, &rx, &ry);
+    if (rc) return herr(rc);
+
+    // output header (:555-561): binned dimensions whenever binning != 1
+    host::FortranWriter out(nml.datafile);
+    if (!out.ok()) return fail(EBSD_EIO, std::string("cannot create output file '") + nml.datafile + "'");
+    int32_t hdr[3] = {nml.numsx, nml.numsy, (int32_t)numeuler};
+    if (nml.binning != 1) {
+        hdr[0] = nml.numsx / nml.binning;
+        hdr[1] = nml.numsy / nml.binning;
+    }
+    if (!out.write(hdr, sizeof hdr)) return fail(EBSD_EIO, "output header write failed");
+
+    const auto t0 = std::chrono::steady_clock::now();                 // Time_start (:567)
+    const size_t rec = (size_t)rx * ry;
+    const int64_t chunk = std::max<int64_t>(
+        1, std::min<int64_t>(numeuler, (int64_t)((size_t(256) << 20) / (rec * sizeof(float)))));
+    PinnedGuard pg;
+    for (int b = 0; b < 2; ++b) {
+        cudaError_t e = cudaMallocHost(&pg.p[b], std::max<size_t>(1, chunk * rec) * sizeof(float));
+        if (e != cudaSuccess) return fail(EBSD_ENOMEM, "pinned output buffer");
+    }
+    std::thread writer;
+    bool write_ok = true;
+    for (int64_t o0 = 0, c = 0; o0 < numeuler; o0 += chunk, ++c) {
+        const int64_t m = std::min(chunk, numeuler - o0);
+        float* buf = pg.p[c & 1];
+        rc = ebsd_forward(h, quats.data() + 4 * o0, m, &epi, buf);
+        if (rc) {
+            if (writer.joinable()) writer.join();
+            return herr(rc);
+        }
+        if (writer.joinable()) writer.join();
+        writer = std::thread([&out, &write_ok, buf, m, rec] {
+            for (int64_t k = 0; k < m && write_ok; ++k)                // one record per pattern
+                write_ok = out.write(buf + (size_t)k * rec, rec * sizeof(float));
+        });
+    }
+    if (writer.joinable()) writer.join();
+    if (!write_ok || !out.close()) return fail(EBSD_EIO, "output file write failed");
+    const double secs =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    say("  Total computation time [s] %.3f\n", secs);                 // Time_stop (:669)
+    say("  Time per step/pixel [s] %10.6f\n", numeuler > 0 ? secs / (double)numeuler : 0.0);
+    return EBSD_OK;
+}

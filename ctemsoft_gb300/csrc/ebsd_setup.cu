@@ -1,0 +1,253 @@
+// Per-detector and per-master set-up kernels: master re-layout, detector
+// direction cosines, Monte-Carlo energy weights and the num_el sum.
+// Compiled with -fmad=false (see ebsd_device.cuh).
+#include "ebsd_device.cuh"
+#include "ebsd_internal.h"
+
+namespace ebsd {
+
+// sr = sum(srtmp,4) (CTEMEBSD.f90:404) restricted to bins e0..e0+nsel-1 and
+// re-laid out energy-fastest: il[(y*gx + x)*NV*4 + k], zero padded to NV*4.
+// The Fortran source is srtmp(x, y, E, set), x fastest.
+__global__ void k_master_relayout(const float* __restrict__ raw, int gx, int gy, int nE,
+                                  int numset, int e0, int nsel, int NV, float* __restrict__ il)
+{
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nodes = (int64_t)gx * gy;
+    if (node >= nodes) return;
+    const int64_t plane = nodes;               // elements per energy bin
+    const int64_t setstride = plane * nE;      // elements per atom set
+    float* dst = il + node * (int64_t)NV * 4;
+    for (int k = 0; k < NV * 4; ++k) {
+        float s = 0.0f;
+        if (k < nsel) {
+            const float* src = raw + (int64_t)(e0 + k) * plane + node;
+            for (int st = 0; st < numset; ++st) s = s + src[st * setstride];
+        }
+        dst[k] = s;
+    }
+}
+
+cudaError_t launch_master_relayout(const float* raw, int npx, int npy, int nE, int numset,
+                                   int e0, int nsel, int NV, float4* il, cudaStream_t s)
+{
+    const int gx = 2 * npx + 1, gy = 2 * npy + 1;
+    const int64_t nodes = (int64_t)gx * gy;
+    const int bs = 256;
+    const unsigned blocks = (unsigned)((nodes + bs - 1) / bs);
+    k_master_relayout<<<blocks, bs, 0, s>>>(raw, gx, gy, nE, numset, e0, nsel, NV,
+                                             reinterpret_cast<float*>(il));
+    return cudaGetLastError();
+}
+
+// Detector direction cosines, CTEMEBSD.f90:416-452.  ca/sa are cos/sin of
+// alp (:422-424) computed on the host as the reference does.  Pixel p =
+// i + numsx*j (Fortran rgx(i,j)).
+__global__ void k_detector(float L, float delta, int numsx, int numsy, float xpc, float ypc,
+                           float ca, float sa, float4* __restrict__ rg)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= numsx || j >= numsy) return;
+    const float scin_x = -((xpc - (1.0f - (float)numsx) * 0.5f - (float)i) * delta);  // :418
+    const float scin_y = (ypc - (1.0f - (float)numsy) * 0.5f - (float)j) * delta;     // :419
+    const float L2 = L * L;
+    const float sx = L2 + scin_y * scin_y;                                              // :435
+    const float Ls = ca * scin_y + L * sa;
+    const float Lc = -(sa * scin_y) + L * ca;
+    const float rhos = 1.0f / sqrtf(sx + scin_x * scin_x);                              // :439
+    float x = Ls * rhos, y = scin_x * rhos, z = Lc * rhos;
+    float n = x * x;                                                                     // :448
+    n = n + y * y;
+    n = n + z * z;
+    n = sqrtf(n);
+    rg[(int64_t)j * numsx + i] = make_float4(x / n, y / n, z / n, 0.0f);
+}
+
+cudaError_t launch_detector(const ebsd_geometry& g, float ca, float sa, float4* rg,
+                            cudaStream_t s)
+{
+    dim3 grid((g.numsx + 127) / 128, g.numsy);
+    k_detector<<<grid, 128, 0, s>>>(g.L, g.delta, g.numsx, g.numsy, g.xpc, g.ypc, ca, sa, rg);
+    return cudaGetLastError();
+}
+
+// accum_e_detector for bins e0..e0+nsel-1, CTEMEBSD.f90:483-510 (the 0.25
+// factor of :510 included).  accum_e(k, -nsx:nsx, -nsy:nsy), k fastest.
+//
+// Two evaluations per pixel:
+//  * Wref: the reference's single-precision arithmetic on the single-precision
+//    direction cosines rg; it only feeds num_el (:516), so the intensity
+//    prefactor is the reference's;
+//  * W: the weights the pattern kernels use.  With fp64 != 0 they are
+//    evaluated in binary64 from the geometry (direction, Lambert map and
+//    bilinear interpolation, as an FP64 re-evaluation of :416-510) and
+//    rounded once; the sparse integer histogram makes the single-precision
+//    weights carry ~1e-4 relative position noise, which binary64 removes.
+//    With fp64 == 0, W = Wref.
+// Both are stored as NV float4 planes of P pixels.
+struct WeightsGeom {
+    double L, delta, xpc, ypc, ca, sa;
+    int numsx, numsy;
+};
+
+__device__ __forceinline__ void cell_f64(double ixy, int np, double& d, int& i0)
+{
+    const int ni = (int)((double)np + ixy) - np;
+    d = ixy - (double)ni;
+    i0 = ni + np;
+    i0 = i0 < 0 ? 0 : (i0 > 2 * np ? 2 * np : i0);
+}
+
+__global__ void k_weights(const float4* __restrict__ rg, int P, const int32_t* __restrict__ acc,
+                          int nE, int nsx, int nsy, float sclmc, float spi2, int e0, int nsel,
+                          int NV, int fp64, WeightsGeom gd, float4* __restrict__ W,
+                          float4* __restrict__ Wref)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int64_t gxm = 2 * nsx + 1;
+
+    // --- reference single precision (feeds num_el) ---
+    const float4 r = rg[p];
+    float d0 = r.x, d1 = r.y, d2 = r.z;
+    if (d2 < 0.0f) {                                                       // :488
+        d0 = -d0;
+        d1 = -d1;
+        d2 = -d2;
+    }
+    float X, Y;
+    lambert_inverse(d0, d1, d2, spi2, X, Y);                               // :490
+    const float ixy0 = sclmc * Y;                                          // swap :491-493
+    const float ixy1 = -(sclmc * X);
+    float dx, dy;
+    int nix, niy;
+    const int ix0 = lambert_cell(ixy0, nsx, dx, nix);                      // :495-500
+    const int iy0 = lambert_cell(ixy1, nsy, dy, niy);
+    const float dxm = 1.0f - dx, dym = 1.0f - dy;
+    const int ix1 = min(ix0 + 1, 2 * nsx), iy1 = min(iy0 + 1, 2 * nsy);
+    const int32_t* a00 = acc + ((int64_t)iy0 * gxm + ix0) * nE + e0;
+    const int32_t* a10 = acc + ((int64_t)iy0 * gxm + ix1) * nE + e0;
+    const int32_t* a01 = acc + ((int64_t)iy1 * gxm + ix0) * nE + e0;
+    const int32_t* a11 = acc + ((int64_t)iy1 * gxm + ix1) * nE + e0;
+
+    // --- binary64 re-evaluation (feeds the pattern kernels) ---
+    double Dx = 0.0, Dy = 0.0;
+    int jx0 = 0, jy0 = 0, jx1 = 0, jy1 = 0;
+    if (fp64) {
+        const int i = p % gd.numsx, j = p / gd.numsx;
+        const double sxp = -(gd.xpc - (1.0 - gd.numsx) * 0.5 - i) * gd.delta;
+        const double syp = (gd.ypc - (1.0 - gd.numsy) * 0.5 - j) * gd.delta;
+        const double Ls = gd.ca * syp + gd.L * gd.sa;
+        const double Lc = -gd.sa * syp + gd.L * gd.ca;
+        const double rh = 1.0 / sqrt(gd.L * gd.L + syp * syp + sxp * sxp);
+        double x = Ls * rh, y = sxp * rh, z = Lc * rh;
+        const double n = sqrt(x * x + y * y + z * z);
+        x /= n;
+        y /= n;
+        z /= n;
+        if (z < 0.0) {
+            x = -x;
+            y = -y;
+            z = -z;
+        }
+        const double spi2d = 0.88622692545275801365;  // sqrt(pi)/2
+        double LX = 0.0, LY = 0.0;
+        const double s2 = x * x + y * y + z * z;
+        if (!(fabs(1.0 - s2) > 1.0e-12) && fabs(z) != 1.0) {
+            if (fabs(y) <= fabs(x)) {
+                const double q = copysign(sqrt(2.0 * (1.0 - z)), x);
+                LX = q * spi2d;
+                LY = q * atan(y / x) / spi2d;
+            } else {
+                const double q = copysign(sqrt(2.0 * (1.0 - z)), y);
+                LX = q * atan(x / y) / spi2d;
+                LY = q * spi2d;
+            }
+        }
+        const double scl = (double)nsx / 1.25331413731550025121;  // nsx / sqrt(pi/2)
+        cell_f64(scl * LY, nsx, Dx, jx0);
+        cell_f64(-(scl * LX), nsy, Dy, jy0);
+        jx1 = min(jx0 + 1, 2 * nsx);
+        jy1 = min(jy0 + 1, 2 * nsy);
+    }
+    const int32_t* b00 = acc + ((int64_t)jy0 * gxm + jx0) * nE + e0;
+    const int32_t* b10 = acc + ((int64_t)jy0 * gxm + jx1) * nE + e0;
+    const int32_t* b01 = acc + ((int64_t)jy1 * gxm + jx0) * nE + e0;
+    const int32_t* b11 = acc + ((int64_t)jy1 * gxm + jx1) * nE + e0;
+    const double Dxm = 1.0 - Dx, Dym = 1.0 - Dy;
+
+    for (int c = 0; c < NV; ++c) {
+        float v[4], u[4];
+        for (int t = 0; t < 4; ++t) {
+            const int k = 4 * c + t;
+            float w = 0.0f, wd = 0.0f;
+            if (k < nsel) {
+                w = (float)a00[k] * dxm * dym + (float)a10[k] * dx * dym +      // :503-506
+                    (float)a01[k] * dxm * dy + (float)a11[k] * dx * dy;
+                w = w * 0.25f;                                                  // :510
+                if (fp64)
+                    wd = (float)(0.25 * ((double)b00[k] * Dxm * Dym + (double)b10[k] * Dx * Dym +
+                                         (double)b01[k] * Dxm * Dy + (double)b11[k] * Dx * Dy));
+                else
+                    wd = w;
+            }
+            v[t] = w;
+            u[t] = wd;
+        }
+        Wref[(int64_t)c * P + p] = make_float4(v[0], v[1], v[2], v[3]);
+        W[(int64_t)c * P + p] = make_float4(u[0], u[1], u[2], u[3]);
+    }
+}
+
+cudaError_t launch_weights(const float4* rg, int P, const int32_t* accum_e, int nE, int nsx,
+                           int nsy, float sclmc, float spi2, int e0, int nsel, int NV, int fp64,
+                           const ebsd_geometry& g, float4* W, float4* Wref, cudaStream_t s)
+{
+    WeightsGeom gd;
+    const double dtor = (double)0.0174533f;
+    const double alp = 0.5 * 3.141592653589793238 - ((double)(float)g.sig - (double)g.thetac) * dtor;
+    gd.L = g.L;
+    gd.delta = g.delta;
+    gd.xpc = g.xpc;
+    gd.ypc = g.ypc;
+    gd.ca = cos(alp);
+    gd.sa = sin(alp);
+    gd.numsx = g.numsx;
+    gd.numsy = g.numsy;
+    const int bs = 256;
+    k_weights<<<(P + bs - 1) / bs, bs, 0, s>>>(rg, P, accum_e, nE, nsx, nsy, sclmc, spi2, e0,
+                                               nsel, NV, fp64, gd, W, Wref);
+    return cudaGetLastError();
+}
+
+// num_el = nint(sum(accum_e_detector)), CTEMEBSD.f90:516.  gfortran sums
+// the array sequentially in single precision in memory order (bin fastest,
+// then x, then y); bins outside the window add exact zeros.  One thread
+// reproduces that order; it runs once per detector.
+__global__ void k_num_el(const float4* __restrict__ W, int P, int nsel, int NV,
+                         float* __restrict__ out)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    float s = 0.0f;
+    for (int p = 0; p < P; ++p) {
+        for (int c = 0; c < NV; ++c) {
+            const float4 w = W[(int64_t)c * P + p];
+            const int k = 4 * c;
+            if (k + 0 < nsel) s = s + w.x;
+            if (k + 1 < nsel) s = s + w.y;
+            if (k + 2 < nsel) s = s + w.z;
+            if (k + 3 < nsel) s = s + w.w;
+        }
+    }
+    *out = s;
+}
+
+cudaError_t launch_num_el(const float4* W, int P, int nsel, int NV, float* sum_out,
+                          cudaStream_t s)
+{
+    k_num_el<<<1, 32, 0, s>>>(W, P, nsel, NV, sum_out);
+    return cudaGetLastError();
+}
+
+}  // namespace ebsd

@@ -1,0 +1,213 @@
+/*
+ * ebsd_gpu.h -- C ABI of libebsdgpu.so, a GB300 (sm_103a) implementation of
+ * the EBSD pattern loop of CTEMsoft's CTEMEBSD program.
+ *
+ * The reference is a Fortran program; its pattern loop has no library API.
+ * These entry points replace, one for one, the stages of
+ * ComputeEBSDPatterns (src_programs/CTEMEBSD.f90:87-672) that a Fortran
+ * host would hand to the GPU through ISO_C_BINDING, and the whole program
+ * (ebsd_run_namelist).  Citations are file:line in the reference tree.
+ *
+ * Conventions
+ *   - Every int-returning call returns EBSD_OK (0) or a negative EBSD_E*
+ *     code, and never exits or aborts; ebsd_last_error() gives the message.
+ *   - Arrays are passed in Fortran (column-major) order, exactly as the
+ *     reference declares them; nothing is transposed on the host.
+ *   - Pattern pointers may be host (pageable or pinned) or device memory;
+ *     the library inspects each pointer.  Pointers are borrowed for the
+ *     duration of the call only.
+ *   - One handle owns one device, one CUDA stream and its device buffers.
+ *     A handle is not thread-safe; separate handles may run concurrently.
+ */
+#ifndef EBSD_GPU_H
+#define EBSD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EBSD_OK 0
+#define EBSD_EINVAL (-1)       /* bad argument or inconsistent sizes */
+#define EBSD_ECUDA (-2)        /* CUDA runtime error */
+#define EBSD_ENOMEM (-3)       /* device or host allocation failed */
+#define EBSD_ESTATE (-4)       /* call made before its prerequisites */
+#define EBSD_EIO (-5)          /* file could not be opened, read or written */
+#define EBSD_EFORMAT (-6)      /* file content does not match the format */
+#define EBSD_EUNSUPPORTED (-7) /* valid input outside what this build supports */
+#define EBSD_ETIMEOUT (-8)     /* a bounded device-side wait gave up */
+
+/* Scaling modes of CTEMEBSD.f90:195,630-658 (namelist scalingmode). */
+#define EBSD_SCALING_NOT 0 /* 'not': full-size pattern, no binning, no gamma */
+#define EBSD_SCALING_LIN 1 /* 'lin': binning only */
+#define EBSD_SCALING_GAM 2 /* 'gam': binning, then pattern**gammavalue */
+
+typedef struct ebsd_handle ebsd_handle;
+
+/* Detector geometry: namelist EBSDdata (CTEMEBSD.f90:112-124,169-171) plus
+ * the Monte-Carlo sample tilt sig read from the MC file (:344-345). */
+typedef struct {
+    float L;       /* scintillator distance [um] */
+    float thetac;  /* detector tilt below horizontal [deg] */
+    float delta;   /* pixel size on the scintillator [um] */
+    int32_t numsx; /* pixels along x */
+    int32_t numsy; /* pixels along y */
+    float xpc;     /* pattern centre x [pixels] */
+    float ypc;     /* pattern centre y [pixels] */
+    double sig;    /* sample tilt from the MC file [deg] */
+} ebsd_geometry;
+
+/* What happens to each pattern after the gather (CTEMEBSD.f90:608-658). */
+typedef struct {
+    double prefactor;    /* :545, see ebsd_prefactor() */
+    int32_t binning;     /* 1, 2, 4 or 8 (:197) */
+    int32_t scalingmode; /* EBSD_SCALING_* */
+    float gammavalue;    /* exponent for EBSD_SCALING_GAM */
+    int32_t poisson;     /* 0: no noise; 1: Poisson noise (:611-615) */
+    uint64_t seed;       /* noise seed (counter-based: results do not depend
+                            on launch shape or chunking) */
+} ebsd_epilogue;
+
+/* Library version, major*10000 + minor*100 + patch. */
+int ebsd_version(void);
+
+/* Create a handle on CUDA device `device`.  Replaces the allocations of
+ * CTEMEBSD.f90:394,431,477,534. */
+int ebsd_create(ebsd_handle** out, int device);
+
+/* Release every device and host resource of the handle (NULL is a no-op). */
+void ebsd_destroy(ebsd_handle* h);
+
+/* Message for the last failed call on `h`, or for the last failed
+ * ebsd_create / file call on this thread when h is NULL.  Never NULL. */
+const char* ebsd_last_error(const ebsd_handle* h);
+
+/* Run the handle's work on an existing CUDA stream (cudaStream_t passed as
+ * void*); NULL restores the handle's own stream. */
+int ebsd_set_stream(ebsd_handle* h, void* stream);
+
+/* Tuning and precision options (no reference counterpart; defaults keep
+ * the behaviour documented here):
+ *   "weights_fp64"   1 (default): the detector energy weights of
+ *                    CTEMEBSD.f90:483-510 are evaluated in binary64 and
+ *                    rounded once; 0: the reference's single precision.
+ *                    num_el (:516) always uses the reference's arithmetic.
+ *                    Takes effect at the next ebsd_set_detector.
+ *   "tile_y"         pattern-kernel CTA height in pixels: 4, 8 (default), 16.
+ *   "orient_per_cta" orientations per CTA, 1..64 (default 4). */
+int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value);
+
+/* Master pattern upload.  sr is the host array srtmp(-npx:npx,-npy:npy,nE,
+ * numset) of CTEMEBSD.f90:394-400 (Fortran order, x fastest); the atom sets
+ * are summed in set order as sr = sum(srtmp,4) at :404. */
+int ebsd_set_master(ebsd_handle* h, const float* sr, int32_t npx, int32_t npy, int32_t nE,
+                    int32_t numset);
+
+/* Detector set-up: the scintillator direction cosines (CTEMEBSD.f90:416-452)
+ * and the Monte-Carlo energy weights accum_e_detector (:476-510) for bins
+ * Emin..Emax (1-based, inclusive, from ebsd_energy_window).  accum_e is the
+ * host array accum_e(numEbins,-nsx:nsx,-nsy:nsy) (:348-349).  *num_el
+ * receives nint(sum(accum_e_detector)) of :516 (may be NULL).  The master
+ * must be set first (its nE must equal numEbins, :388-393). */
+int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const int32_t* accum_e,
+                      int32_t nsx, int32_t nsy, int32_t numEbins, int32_t Emin, int32_t Emax,
+                      int32_t* num_el);
+
+/* Energy window of CTEMEBSD.f90:361-367 (1-based bin indices). */
+int ebsd_energy_window(float energymin, float energymax, double Ehistmin, double Ebinsize,
+                       int32_t numEbins, int32_t* Emin, int32_t* Emax);
+
+/* Intensity prefactor of CTEMEBSD.f90:545. */
+double ebsd_prefactor(double beamcurrent, double dwelltime, int32_t num_el);
+
+/* Size of one output record for epilogue e: (numsx,numsy) for 'not' or
+ * binning 1, else (numsx/binning, numsy/binning) (:524-525,654-658). */
+int ebsd_output_dims(const ebsd_handle* h, const ebsd_epilogue* e, int32_t* nx, int32_t* ny);
+
+/* The pattern loop, CTEMEBSD.f90:573-658: for each of the n quaternions
+ * (scalar first, n x 4 floats, quatang(4,numeuler) of :270-273) compute
+ * one pattern, apply e, and write record o at out + o*nx*ny (nx*ny from
+ * ebsd_output_dims, x fastest).  quats/out may each be host or device. */
+int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
+                 float* out);
+
+/* Lambert cells of the loop (CTEMEBSD.f90:584-598) for n quaternions:
+ * nix/niy (grid indices in -npx..npx) and the scaled Lambert coordinates
+ * ixy0/ixy1, each [n][numsy][numsx].  Host or device pointers.  For parity
+ * checking of the cell indices. */
+int ebsd_cells(ebsd_handle* h, const float* quats, int64_t n, int32_t* nix, int32_t* niy,
+               float* ixy0, float* ixy1);
+
+/* Copy the detector weights accum_e_detector(numEbins,numsx,numsy) (zero
+ * outside Emin..Emax) and direction cosines rgx/rgy/rgz(numsx,numsy) to
+ * host arrays (any pointer may be NULL).  Diagnostic. */
+int ebsd_get_detector(ebsd_handle* h, float* W, float* rgx, float* rgy, float* rgz);
+
+/* ------------------------------------------------------------------ */
+/* File formats and the drop-in program                                 */
+/* ------------------------------------------------------------------ */
+
+/* The whole CTEMEBSD program (CTEMEBSD.f90:48-672) for namelist file
+ * `nmlfile` (&EBSDdata, :169-205): reads the angle, MC and master files,
+ * computes every pattern on device `device` and writes the unformatted
+ * output file (:555-561,654-658).  Prints the reference's progress lines
+ * unless quiet != 0. */
+int ebsd_run_namelist(const char* nmlfile, int device, int quiet);
+
+/* Header of a CTEMMC output file (CTEMMC.f90:262-277). */
+typedef struct {
+    int32_t numEbins, numzbins, numsx, numsy;
+    int64_t num_el_total;
+    int32_t nthreads;
+    double EkeV, Ehistmin, Ebinsize, depthmax, depthstep;
+    double sig, omega;
+    char MCmode[5];
+} ebsd_mc_header;
+
+/* Read an MC file (CTEMEBSD.f90:319-355).  accum_e may be NULL to read the
+ * header only; otherwise it receives numEbins*numsx*numsy int32. */
+int ebsd_read_mc_file(const char* path, ebsd_mc_header* hdr, int32_t* accum_e);
+
+/* Header of a CTEMEBSDmaster output file (CTEMEBSDmaster.f90:540-568). */
+typedef struct {
+    int32_t npx, npy, nE, numset;
+    char sqorhe[7];
+} ebsd_master_header;
+
+/* Read a master file (CTEMEBSD.f90:378-406).  EkeVs (nE floats), atomtype
+ * (numset int32) and srtmp ((2npx+1)*(2npy+1)*nE*numset floats) may each
+ * be NULL. */
+int ebsd_read_master_file(const char* path, ebsd_master_header* hdr, float* EkeVs,
+                          int32_t* atomtype, float* srtmp);
+
+/* Parsed &EBSDdata namelist with the defaults of CTEMEBSD.f90:179-198. */
+typedef struct {
+    float L, thetac, delta;
+    int32_t numsx, numsy;
+    float xpc, ypc;
+    char anglefile[512], eulerconvention[4], FZfile[512], energyfile[512], datafile[512];
+    double beamcurrent, dwelltime;
+    float energymin, energymax;
+    int32_t binning;
+    float gammavalue;
+    char scalingmode[4];
+    float axisangle[4];
+    /* keys this library adds; defaults keep the reference's behaviour */
+    int32_t poisson; /* default 1: noise on, as the reference always is */
+    int64_t seed;    /* default 1 */
+} ebsd_namelist;
+
+/* Parse a namelist file (Fortran &EBSDdata ... / group). */
+int ebsd_read_namelist(const char* path, ebsd_namelist* nml);
+
+/* Read an angle file (CTEMEBSD.f90:228-288): converts 'eu' rows (degrees;
+ * 'hkl' adds 90 deg to phi1) with eu2qu and applies the optional
+ * axis-angle pre-rotation.  Call with quats == NULL to get *n only. */
+int ebsd_read_angle_file(const char* path, const char* eulerconvention,
+                         const float axisangle[4], int64_t* n, float* quats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EBSD_GPU_H */

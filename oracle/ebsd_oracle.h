@@ -1,0 +1,66 @@
+/*
+ * ebsd_oracle.h -- CPU restatement of CTEMsoft CTEMEBSD's pattern loop.
+ * TEST INFRASTRUCTURE ONLY (the checker); PARITY UNPINNED (the reference has
+ * no tests or fixtures for this path and cannot be compiled here).
+ * See ebsd_oracle.c for the semantics mirrored and the cited source lines.
+ */
+#ifndef EBSD_ORACLE_H
+#define EBSD_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Namelist EBSDdata geometry (CTEMEBSD.f90:112-124) plus the MC tilt sig. */
+typedef struct {
+    float L, thetac, delta;
+    int32_t numsx, numsy;
+    float xpc, ypc;
+    double sig; /* MC file sample tilt, degrees (CTEMMC.f90:272) */
+} oracle_geometry;
+
+int oracle_lambert_inverse_f32(const float xyz[3], float res[2]);
+int oracle_lambert_inverse_f64(const double xyz[3], double res[2]);
+int oracle_lambert_forward_f64(const double xy[2], double res[3]);
+void oracle_quat_mult_f32(const float x[4], const float y[4], float r[4]);
+void oracle_eu2qu_f32(const float e[3], float res[4]);
+void oracle_ax2qu_f32(const float a[4], float res[4]);
+void oracle_angles_to_quats_f32(const float* rows, int64_t n, int mode, int hkl,
+                                const float axisangle[4], float* quats);
+
+void oracle_detector_f32(const oracle_geometry* g, float* rgx, float* rgy, float* rgz);
+void oracle_detector_f64(const oracle_geometry* g, double* rgx, double* rgy, double* rgz);
+
+int32_t oracle_mc_weights_f32(const oracle_geometry* g, const float* rgx, const float* rgy,
+                              const float* rgz, const int32_t* accum_e, int nE, int nsx,
+                              int nsy, int Emin, int Emax, float* W);
+double oracle_mc_weights_f64(const oracle_geometry* g, const double* rgx, const double* rgy,
+                             const double* rgz, const int32_t* accum_e, int nE, int nsx,
+                             int nsy, int Emin, int Emax, double* W);
+double oracle_prefactor(double beamcurrent, double dwelltime, int32_t num_el);
+void oracle_energy_window(float energymin, float energymax, double Ehistmin, double Ebinsize,
+                          int numEbins, int* Emin, int* Emax);
+
+float oracle_master_scale_f32(int npx);
+void oracle_cells_f32(const oracle_geometry* g, const float* rgx, const float* rgy,
+                      const float* rgz, const float* quats, int64_t N, int npx, int npy,
+                      int32_t* nix_out, int32_t* niy_out, float* ixy0_out, float* ixy1_out);
+void oracle_patterns_f32(const oracle_geometry* g, const float* rgx, const float* rgy,
+                         const float* rgz, const float* W, int nE, int Emin, int Emax,
+                         const float* sr, int npx, int npy, const float* quats, int64_t N,
+                         double prefactor, float* out, int nthreads);
+void oracle_patterns_f64(const oracle_geometry* g, const double* rgx, const double* rgy,
+                         const double* rgz, const double* W, int nE, int Emin, int Emax,
+                         const float* sr, int npx, int npy, const float* quats, int64_t N,
+                         double prefactor, double* out, int nthreads);
+void oracle_epilogue_f32(const float* pat, int numsx, int numsy, int binning, int mode,
+                         float gammavalue, float* out);
+void oracle_epilogue_f64(const double* pat, int numsx, int numsy, int binning, int mode,
+                         double gammavalue, double* out);
+int oracle_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

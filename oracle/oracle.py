@@ -1,0 +1,248 @@
+"""ctypes wrapper of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY -- the checker for the GPU library.  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+PARITY UNPINNED: the reference has no tests, fixtures or runnable build for
+this path; see ebsd_oracle.c.
+
+Array layouts (numpy, C order) match the Fortran arrays with the first
+Fortran index last: detector arrays (numsy, numsx), W (numsy, numsx, nE),
+accum_e (2nsy+1, 2nsx+1, nE), master sr (nE, 2npy+1, 2npx+1), patterns
+(N, numsy, numsx).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+
+
+class Geometry(C.Structure):
+    _fields_ = [("L", C.c_float), ("thetac", C.c_float), ("delta", C.c_float),
+                ("numsx", C.c_int32), ("numsy", C.c_int32), ("xpc", C.c_float),
+                ("ypc", C.c_float), ("sig", C.c_double)]
+
+
+_P = C.c_void_p
+_SIGS = {
+    "oracle_lambert_inverse_f32": (C.c_int, [_P, _P]),
+    "oracle_lambert_inverse_f64": (C.c_int, [_P, _P]),
+    "oracle_lambert_forward_f64": (C.c_int, [_P, _P]),
+    "oracle_quat_mult_f32": (None, [_P, _P, _P]),
+    "oracle_eu2qu_f32": (None, [_P, _P]),
+    "oracle_ax2qu_f32": (None, [_P, _P]),
+    "oracle_angles_to_quats_f32": (None, [_P, C.c_int64, C.c_int, C.c_int, _P, _P]),
+    "oracle_detector_f32": (None, [C.POINTER(Geometry), _P, _P, _P]),
+    "oracle_detector_f64": (None, [C.POINTER(Geometry), _P, _P, _P]),
+    "oracle_mc_weights_f32": (C.c_int32, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int, C.c_int,
+                                          C.c_int, C.c_int, C.c_int, _P]),
+    "oracle_mc_weights_f64": (C.c_double, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int,
+                                           C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "oracle_prefactor": (C.c_double, [C.c_double, C.c_double, C.c_int32]),
+    "oracle_energy_window": (None, [C.c_float, C.c_float, C.c_double, C.c_double, C.c_int,
+                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "oracle_master_scale_f32": (C.c_float, [C.c_int]),
+    "oracle_cells_f32": (None, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int64, C.c_int, C.c_int,
+                                _P, _P, _P, _P]),
+    "oracle_patterns_f32": (None, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int, C.c_int,
+                                   C.c_int, _P, C.c_int, C.c_int, _P, C.c_int64, C.c_double, _P,
+                                   C.c_int]),
+    "oracle_patterns_f64": (None, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int, C.c_int,
+                                   C.c_int, _P, C.c_int, C.c_int, _P, C.c_int64, C.c_double, _P,
+                                   C.c_int]),
+    "oracle_epilogue_f32": (None, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _P]),
+    "oracle_epilogue_f64": (None, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _P]),
+    "oracle_max_threads": (C.c_int, []),
+}
+
+_lib = None
+
+
+def build() -> Path:
+    src = HERE / "ebsd_oracle.c"
+    if not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime,
+                                                      (HERE / "ebsd_oracle.h").stat().st_mtime):
+        subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data if a is not None else None
+
+
+def geometry(g: dict) -> Geometry:
+    return Geometry(g["L"], g["thetac"], g["delta"], g["numsx"], g["numsy"], g["xpc"], g["ypc"],
+                    g["sig"])
+
+
+def lambert_inverse_f32(xyz):
+    v = np.asarray(xyz, np.float32)
+    r = np.zeros(2, np.float32)
+    ierr = lib().oracle_lambert_inverse_f32(_p(v), _p(r))
+    return r, ierr
+
+
+def lambert_inverse_f64(xyz):
+    v = np.asarray(xyz, np.float64)
+    r = np.zeros(2, np.float64)
+    ierr = lib().oracle_lambert_inverse_f64(_p(v), _p(r))
+    return r, ierr
+
+
+def lambert_forward_f64(xy):
+    v = np.asarray(xy, np.float64)
+    r = np.zeros(3, np.float64)
+    ierr = lib().oracle_lambert_forward_f64(_p(v), _p(r))
+    return r, ierr
+
+
+def quat_mult_f32(x, y):
+    a, b = np.asarray(x, np.float32), np.asarray(y, np.float32)
+    r = np.zeros(4, np.float32)
+    lib().oracle_quat_mult_f32(_p(a), _p(b), _p(r))
+    return r
+
+
+def eu2qu_f32(e):
+    a = np.asarray(e, np.float32)
+    r = np.zeros(4, np.float32)
+    lib().oracle_eu2qu_f32(_p(a), _p(r))
+    return r
+
+
+def ax2qu_f32(a):
+    v = np.asarray(a, np.float32)
+    r = np.zeros(4, np.float32)
+    lib().oracle_ax2qu_f32(_p(v), _p(r))
+    return r
+
+
+def angles_to_quats(rows, mode: str, hkl: bool = False, axisangle=(0, 0, 0, 0)):
+    r = np.ascontiguousarray(rows, np.float32)
+    n = r.shape[0]
+    q = np.zeros((n, 4), np.float32)
+    aa = np.asarray(axisangle, np.float32)
+    lib().oracle_angles_to_quats_f32(_p(r), n, 0 if mode == "eu" else 1, int(hkl), _p(aa), _p(q))
+    return q
+
+
+def energy_window(energymin, energymax, Ehistmin, Ebinsize, numEbins):
+    a, b = C.c_int(), C.c_int()
+    lib().oracle_energy_window(energymin, energymax, Ehistmin, Ebinsize, numEbins, C.byref(a),
+                               C.byref(b))
+    return a.value, b.value
+
+
+def prefactor(beamcurrent, dwelltime, num_el):
+    return lib().oracle_prefactor(beamcurrent, dwelltime, num_el)
+
+
+class Detector:
+    """Detector set-up in FP32 (reference semantics) and FP64."""
+
+    def __init__(self, geom: dict, accum_e: np.ndarray, Emin: int, Emax: int):
+        self.geom = dict(geom)
+        g = geometry(geom)
+        self._g = g
+        ny, nx = geom["numsy"], geom["numsx"]
+        self.rg32 = [np.zeros((ny, nx), np.float32) for _ in range(3)]
+        lib().oracle_detector_f32(C.byref(g), *(_p(a) for a in self.rg32))
+        self.rg64 = [np.zeros((ny, nx), np.float64) for _ in range(3)]
+        lib().oracle_detector_f64(C.byref(g), *(_p(a) for a in self.rg64))
+        acc = np.ascontiguousarray(accum_e, np.int32)
+        gy, gx, nE = acc.shape
+        self.nE, self.Emin, self.Emax = nE, Emin, Emax
+        self.nsx, self.nsy = (gx - 1) // 2, (gy - 1) // 2
+        self.W32 = np.zeros((ny, nx, nE), np.float32)
+        self.num_el = lib().oracle_mc_weights_f32(C.byref(g), *(_p(a) for a in self.rg32), _p(acc),
+                                                  nE, self.nsx, self.nsy, Emin, Emax, _p(self.W32))
+        self.W64 = np.zeros((ny, nx, nE), np.float64)
+        self.Wsum64 = lib().oracle_mc_weights_f64(C.byref(g), *(_p(a) for a in self.rg64),
+                                                  _p(acc), nE, self.nsx, self.nsy, Emin, Emax,
+                                                  _p(self.W64))
+
+    def cells(self, quats, npx, npy=None):
+        npy = npx if npy is None else npy
+        q = np.ascontiguousarray(quats, np.float32)
+        n = q.shape[0]
+        ny, nx = self.geom["numsy"], self.geom["numsx"]
+        nix = np.zeros((n, ny, nx), np.int32)
+        niy = np.zeros_like(nix)
+        i0 = np.zeros((n, ny, nx), np.float32)
+        i1 = np.zeros_like(i0)
+        lib().oracle_cells_f32(C.byref(self._g), *(_p(a) for a in self.rg32), _p(q), n, npx, npy,
+                               _p(nix), _p(niy), _p(i0), _p(i1))
+        return nix, niy, i0, i1
+
+    def patterns_f32(self, sr, quats, prefactor, nthreads=1):
+        s = np.ascontiguousarray(sr, np.float32)
+        nE, gy, gx = s.shape
+        q = np.ascontiguousarray(quats, np.float32)
+        n = q.shape[0]
+        ny, nx = self.geom["numsy"], self.geom["numsx"]
+        out = np.zeros((n, ny, nx), np.float32)
+        lib().oracle_patterns_f32(C.byref(self._g), *(_p(a) for a in self.rg32), _p(self.W32),
+                                  self.nE, self.Emin, self.Emax, _p(s), (gx - 1) // 2,
+                                  (gy - 1) // 2, _p(q), n, prefactor, _p(out), nthreads)
+        return out
+
+    def patterns_f64(self, sr, quats, prefactor, nthreads=1):
+        s = np.ascontiguousarray(sr, np.float32)
+        nE, gy, gx = s.shape
+        q = np.ascontiguousarray(quats, np.float32)
+        n = q.shape[0]
+        ny, nx = self.geom["numsy"], self.geom["numsx"]
+        out = np.zeros((n, ny, nx), np.float64)
+        lib().oracle_patterns_f64(C.byref(self._g), *(_p(a) for a in self.rg64), _p(self.W64),
+                                  self.nE, self.Emin, self.Emax, _p(s), (gx - 1) // 2,
+                                  (gy - 1) // 2, _p(q), n, prefactor, _p(out), nthreads)
+        return out
+
+
+def epilogue_f32(pat, binning, mode, gammavalue):
+    p = np.ascontiguousarray(pat, np.float32)
+    ny, nx = p.shape
+    if mode == 0 or binning == 1:
+        out = np.zeros((ny, nx), np.float32)
+    else:
+        out = np.zeros((ny // binning, nx // binning), np.float32)
+    lib().oracle_epilogue_f32(_p(p), nx, ny, binning, mode, gammavalue, _p(out))
+    return out
+
+
+def epilogue_f64(pat, binning, mode, gammavalue):
+    p = np.ascontiguousarray(pat, np.float64)
+    ny, nx = p.shape
+    if mode == 0:
+        out = np.zeros((ny, nx), np.float64)
+    else:
+        out = np.zeros((ny // binning, nx // binning), np.float64)
+    lib().oracle_epilogue_f64(_p(p), nx, ny, binning, mode, gammavalue, _p(out))
+    return out
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())
+
+
+def host_threads() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()

@@ -1,0 +1,266 @@
+"""GPU parity of the pattern loop against the CPU oracle, through the C ABI."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from ctemsoft_gb300 import capi, synth
+from tests.conftest import workload_data
+from tests.parity import TOL_FP64, TOL_REF, cell_report, rel_errors
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle():
+    from oracle import oracle as O
+    return O
+
+
+def _setup(wl, Emin=1, Emax=None, fp64=True, master=None, acc=None):
+    O = _oracle()
+    sr, accum = workload_data(wl)
+    if master is not None:
+        sr = master
+    if acc is not None:
+        accum = acc
+    Emax = wl.nEbins if Emax is None else Emax
+    h = capi.Handle(0)
+    h.set_option("weights_fp64", int(fp64))
+    h.set_master(sr)
+    num_el = h.set_detector(wl.geometry(), accum, Emin, Emax)
+    det = O.Detector(wl.geometry(), accum, Emin, Emax)
+    return h, det, sr, num_el
+
+
+@pytest.mark.parametrize("wl", [synth.tiny(), synth.tiny(seed=11, numsx=37, numsy=29, npx=33,
+                                                          nE=7, phase="Ti")],
+                         ids=["tiny-Ni", "tiny-Ti-ragged"])
+def test_tiny_parity(built, wl):
+    h, det, sr, num_el = _setup(wl)
+    q = wl.quaternions(wl.n_orient)
+    assert num_el == det.num_el
+    # Lambert cells: bit-exact except at cell edges
+    rep = cell_report(h.cells(q), det.cells(q, wl.npx), wl.npx, wl.npx)
+    assert rep["non_edge"] == 0, rep
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    epi = capi.epilogue(pref)
+    gpu = h.forward(q, epi)
+    p64 = det.patterns_f64(sr, q, pref)
+    p32 = det.patterns_f32(sr, q, pref)
+    l2, mx = rel_errors(gpu, p64)
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64, (l2.max(), mx.max())
+    l2, mx = rel_errors(gpu, p32)
+    assert l2.max() <= TOL_REF and mx.max() <= TOL_REF, (l2.max(), mx.max())
+    h.close()
+
+
+def test_tiny_reference_weights_mode(built):
+    """With single-precision weights the GPU follows the FP32 reference
+    operation by operation; differences come only from atanf."""
+    wl = synth.tiny()
+    h, det, sr, num_el = _setup(wl, fp64=False)
+    q = wl.quaternions(wl.n_orient)
+    W, rgx, rgy, rgz = h.get_detector(wl.nEbins)
+    assert np.array_equal(rgx, det.rg32[0]) and np.array_equal(rgy, det.rg32[1]) \
+        and np.array_equal(rgz, det.rg32[2])
+    l2, mx = rel_errors(W[None], det.W32[None])
+    assert mx.max() < 1e-5
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    gpu = h.forward(q, capi.epilogue(pref))
+    p32 = det.patterns_f32(sr, q, pref)
+    l2, mx = rel_errors(gpu, p32)
+    assert mx.max() <= 1e-5, mx.max()
+    # most pixels bit-identical to the FP32 reference restatement
+    assert np.mean(gpu == p32) > 0.5
+    h.close()
+
+
+def test_c1_parity(built):
+    """80x60 detector, 501^2 x 11 master, 100 orientations, gamma 0.33."""
+    O = _oracle()
+    wl = synth.C1
+    h, det, sr, num_el = _setup(wl)
+    q = wl.quaternions()
+    assert num_el == det.num_el
+    rep = cell_report(h.cells(q), det.cells(q, wl.npx), wl.npx, wl.npx)
+    print("C1 cells", rep)
+    assert rep["non_edge"] == 0, rep
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    raw = h.forward(q, capi.epilogue(pref))
+    p64 = det.patterns_f64(sr, q, pref, nthreads=O.max_threads())
+    p32 = det.patterns_f32(sr, q, pref, nthreads=O.max_threads())
+    l2, mx = rel_errors(raw, p64)
+    print("C1 vs FP64: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64
+    l2, mx = rel_errors(raw, p32)
+    assert l2.max() <= TOL_REF and mx.max() <= TOL_REF
+    gam = h.forward(q, capi.epilogue(pref, scalingmode="gam", gammavalue=wl.gammavalue))
+    ref = np.stack([O.epilogue_f64(p, 1, 2, wl.gammavalue) for p in p64])
+    l2, mx = rel_errors(gam, ref)
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64
+    h.close()
+
+
+@pytest.mark.parametrize("binning", [1, 2, 4, 8])
+@pytest.mark.parametrize("mode", ["not", "lin", "gam"])
+def test_epilogue_binning(built, binning, mode):
+    O = _oracle()
+    wl = synth.tiny(seed=5, numsx=44, numsy=35, npx=30, nE=4, n_orient=5)
+    h, det, sr, num_el = _setup(wl)
+    q = wl.quaternions()
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    out = h.forward(q, capi.epilogue(pref, binning=binning, scalingmode=mode, gammavalue=0.33))
+    p64 = det.patterns_f64(sr, q, pref)
+    m = capi.SCALING[mode]
+    ref = np.stack([O.epilogue_f64(p, binning, m, 0.33) for p in p64])
+    assert out.shape == ref.shape
+    l2, mx = rel_errors(out, ref)
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64, (l2.max(), mx.max())
+    h.close()
+
+
+def test_q_and_minus_q_identical(built):
+    wl = synth.tiny()
+    h, det, sr, num_el = _setup(wl)
+    q = wl.quaternions()
+    epi = capi.epilogue(1.0)
+    assert np.array_equal(h.forward(q, epi), h.forward(-q, epi))
+    h.close()
+
+
+def test_uniform_master(built):
+    """A constant master pattern c gives prefactor * c * sum_k W_k."""
+    wl = synth.tiny()
+    sr, acc = workload_data(wl)
+    const = np.full_like(sr, 2.5)
+    h, det, _, num_el = _setup(wl, master=const)
+    q = wl.quaternions()
+    out = h.forward(q, capi.epilogue(1.0))
+    W, *_ = h.get_detector(wl.nEbins)
+    expect = 2.5 * W.astype(np.float64).sum(axis=-1)
+    np.testing.assert_allclose(out, np.broadcast_to(expect, out.shape), rtol=2e-6, atol=1e-30)
+    h.close()
+
+
+def test_identity_quaternion_is_detector_frame(built):
+    """q = (1,0,0,0) gathers along the detector directions themselves."""
+    wl = synth.tiny()
+    h, det, sr, num_el = _setup(wl)
+    q = np.array([[1, 0, 0, 0]], np.float32)
+    out = h.forward(q, capi.epilogue(1.0))
+    ref = det.patterns_f64(sr, q, 1.0)
+    l2, mx = rel_errors(out, ref)
+    assert mx.max() <= TOL_FP64
+    h.close()
+
+
+def test_device_and_host_buffers_agree(built):
+    torch = pytest.importorskip("torch")
+    wl = synth.tiny()
+    h, det, sr, num_el = _setup(wl)
+    q = wl.quaternions()
+    epi = capi.epilogue(3.0, scalingmode="gam", gammavalue=0.5)
+    host = h.forward(q, epi)
+    dq = torch.from_numpy(q).cuda()
+    dout = torch.empty(host.shape, dtype=torch.float32, device="cuda")
+    h.forward(dq, epi, out=dout)
+    torch.cuda.synchronize()
+    assert np.array_equal(dout.cpu().numpy(), host)
+    pinned = torch.empty(host.shape, dtype=torch.float32).pin_memory()
+    h.forward(q, epi, out=pinned)
+    assert np.array_equal(pinned.numpy(), host)
+    h.close()
+
+
+def test_many_chunks_pageable(built):
+    """More orientations than one device chunk: the double-buffered host
+    path must keep every record in place."""
+    wl = synth.tiny(numsx=640, numsy=480, npx=40, nE=5, n_orient=300)
+    h, det, sr, num_el = _setup(wl)
+    q = wl.quaternions()
+    epi = capi.epilogue(1.0)
+    out = h.forward(q, epi)
+    import torch
+    dout = torch.empty(out.shape, dtype=torch.float32, device="cuda")
+    h.forward(torch.from_numpy(q).cuda(), epi, out=dout)
+    torch.cuda.synchronize()
+    assert np.array_equal(dout.cpu().numpy(), out)
+    sel = [0, 137, 299]
+    ref = det.patterns_f64(sr, q[sel], 1.0)
+    l2, mx = rel_errors(out[sel], ref)
+    assert mx.max() <= TOL_FP64
+    h.close()
+
+
+def test_edge_cases(built):
+    wl = synth.tiny()
+    h, det, sr, num_el = _setup(wl)
+    epi = capi.epilogue(1.0)
+    # zero orientations is a no-op
+    out = h.forward(np.zeros((0, 4), np.float32), epi)
+    assert out.shape == (0, wl.numsy, wl.numsx)
+    # a single orientation
+    q = wl.quaternions(1)
+    assert h.forward(q, epi).shape == (1, wl.numsy, wl.numsx)
+    # non-finite quaternions are rejected before any launch
+    bad = q.copy()
+    bad[0, 2] = np.nan
+    with pytest.raises(capi.EBSDError) as e:
+        h.forward(bad, epi)
+    assert e.value.code == capi.EBSD_EINVAL
+    # unsupported binning
+    with pytest.raises(capi.EBSDError) as e:
+        h.forward(q, capi.epilogue(1.0, binning=3, scalingmode="lin"))
+    assert e.value.code == capi.EBSD_EUNSUPPORTED
+    # a non-unit quaternion is used as given (the reference does not
+    # normalise); the direction is renormalised, so the pattern is the same
+    out2 = h.forward(q * 2.0, epi)
+    ref = det.patterns_f64(sr, q * 2.0, 1.0)
+    l2, mx = rel_errors(out2, ref)
+    assert mx.max() <= TOL_FP64
+    h.close()
+
+
+def test_call_order_and_mismatch_errors(built):
+    wl = synth.tiny()
+    sr, acc = workload_data(wl)
+    h = capi.Handle(0)
+    with pytest.raises(capi.EBSDError) as e:
+        h.forward(wl.quaternions(1), capi.epilogue(1.0))
+    assert e.value.code == capi.EBSD_ESTATE
+    with pytest.raises(capi.EBSDError) as e:
+        h.set_detector(wl.geometry(), acc, 1, wl.nEbins)
+    assert e.value.code == capi.EBSD_ESTATE
+    h.set_master(sr[:-1])  # one energy bin fewer than the MC histogram
+    with pytest.raises(capi.EBSDError) as e:
+        h.set_detector(wl.geometry(), acc, 1, wl.nEbins)
+    assert e.value.code == capi.EBSD_EINVAL and "energy dimension" in str(e.value)
+    h.close()
+
+
+def test_c2_subset_and_properties(built):
+    """640x480 detector, 1001^2 x 11 master: parity on a subset of the
+    10 000 orientations, plus size-independent properties on more."""
+    O = _oracle()
+    wl = synth.C2
+    h, det, sr, num_el = _setup(wl)
+    assert num_el == det.num_el
+    q = wl.quaternions(64)
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    epi = capi.epilogue(pref)
+    out = h.forward(q, epi)
+    sel = np.arange(0, 64, 8)
+    p64 = det.patterns_f64(sr, q[sel], pref, nthreads=O.max_threads())
+    l2, mx = rel_errors(out[sel], p64)
+    print("C2 vs FP64: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64
+    p32 = det.patterns_f32(sr, q[sel[:2]], pref, nthreads=O.max_threads())
+    l2, mx = rel_errors(out[sel[:2]], p32)
+    assert l2.max() <= TOL_REF and mx.max() <= TOL_REF
+    rep = cell_report(h.cells(q[:4]), det.cells(q[:4], wl.npx), wl.npx, wl.npx)
+    print("C2 cells", rep)
+    assert rep["non_edge"] == 0
+    # q and -q, and repeat determinism, on the whole batch
+    assert np.array_equal(out, h.forward(-q, epi))
+    assert np.array_equal(out, h.forward(q, epi))
+    h.close()
