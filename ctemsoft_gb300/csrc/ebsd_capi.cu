@@ -57,6 +57,7 @@ struct ebsd_handle {
 
     LaunchCfg cfg;
     int weights_fp64 = 1;
+    int lambert_accurate = 0;
 };
 
 namespace {
@@ -166,6 +167,7 @@ int fill_params(ebsd_handle* h, const ebsd_epilogue* e, FwdParams& p)
     p.gx = 2 * h->npx + 1;
     p.scl = host::lambert_scale(h->npx);
     p.spi2 = host::lambert_spi2_f();
+    p.accurate = h->lambert_accurate;
     if (e) {
         if (e->scalingmode < EBSD_SCALING_NOT || e->scalingmode > EBSD_SCALING_GAM)
             return set_err(h, EBSD_EINVAL, "scalingmode %d is not 0 ('not'), 1 ('lin') or 2 ('gam')",
@@ -310,6 +312,8 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
         h->weights_fp64 = value != 0;
         if (h->have_detector)
             return set_err(h, EBSD_ESTATE, "weights_fp64 applies at the next ebsd_set_detector");
+    } else if (k == "lambert_accurate") {
+        h->lambert_accurate = value != 0;
     } else if (k == "tile_y") {
         if (value != 4 && value != 8 && value != 16)
             return set_err(h, EBSD_EINVAL, "tile_y must be 4, 8 or 16");

@@ -50,13 +50,14 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
 // Rotated, projected and scaled Lambert coordinates of one pixel for one
 // orientation (CTEMEBSD.f90:584-591).
 __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, float scl,
-                                              float spi2, float& ixy0, float& ixy1)
+                                              float spi2, bool accurate, float& ixy0,
+                                              float& ixy1)
 {
     float d0, d1, d2;
     rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
     normalize_fold(d0, d1, d2);
     float X, Y;
-    lambert_inverse(d0, d1, d2, spi2, X, Y);
+    lambert_inverse(d0, d1, d2, spi2, X, Y, accurate);
     ixy0 = scl * X;
     ixy1 = scl * Y;
 }
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y
         if (inside) {
             const float4 q = ldg4(prm.quats + o);
             float ixy0, ixy1;
-            pixel_lambert(q, r, prm.scl, prm.spi2, ixy0, ixy1);
+            pixel_lambert(q, r, prm.scl, prm.spi2, prm.accurate != 0, ixy0, ixy1);
             float dx, dy;
             int nix, niy;
             const int ix0 = lambert_cell(ixy0, prm.npx, dx, nix);
@@ -136,7 +137,7 @@ __global__ void k_cells(const FwdParams prm)
     const int64_t o = idx / prm.P;
     const int p = (int)(idx - o * prm.P);
     float ixy0, ixy1;
-    pixel_lambert(prm.quats[o], prm.rg[p], prm.scl, prm.spi2, ixy0, ixy1);
+    pixel_lambert(prm.quats[o], prm.rg[p], prm.scl, prm.spi2, prm.accurate != 0, ixy0, ixy1);
     float dx, dy;
     int nix, niy;
     lambert_cell(ixy0, prm.npx, dx, nix);

@@ -39,6 +39,7 @@ struct FwdParams {
     int out_nx, out_ny;
     int poisson;
     uint64_t seed;
+    int accurate;          // cancellation-free 1 - z near the poles
     // diagnostics (cells mode)
     int32_t* nix;
     int32_t* niy;

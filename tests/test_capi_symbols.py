@@ -1,0 +1,81 @@
+"""The C-ABI library loads and exports every function include/*.h declares
+(no compute calls; runs without a GPU)."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from ctemsoft_gb300 import capi
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions() -> list[str]:
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"\b(ebsd_[a-z0-9_]+)\s*\(", text):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for must in ("ebsd_create", "ebsd_destroy", "ebsd_set_master", "ebsd_set_detector",
+                 "ebsd_forward", "ebsd_last_error", "ebsd_run_namelist"):
+        assert must in names
+
+
+def test_every_declared_symbol_is_exported(built):
+    lib = capi.lib()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", str(capi.LIB_PATH)], capture_output=True,
+                         text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    assert set(declared_functions()) <= exported
+
+
+def test_binding_covers_the_header(built):
+    assert set(declared_functions()) == set(capi.exported_symbols())
+
+
+def test_errors_without_side_effects(built):
+    lib = capi.lib()
+    assert lib.ebsd_version() >= 100
+    # null handles and bad arguments are reported, never crash
+    assert lib.ebsd_set_master(None, None, 1, 1, 1, 1) == capi.EBSD_EINVAL
+    assert lib.ebsd_forward(None, None, 1, None, None) == capi.EBSD_EINVAL
+    assert b"null handle" in lib.ebsd_last_error(None)
+    a, b = C.c_int32(), C.c_int32()
+    assert lib.ebsd_energy_window(10.0, 20.0, 10.0, 0.0, 11, C.byref(a), C.byref(b)) == \
+        capi.EBSD_EINVAL
+    lib.ebsd_destroy(None)
+    h = C.c_void_p()
+    rc = lib.ebsd_create(C.byref(h), 0)
+    if rc == capi.EBSD_OK:      # a GPU is present
+        lib.ebsd_destroy(h)
+    else:
+        assert rc in (capi.EBSD_ECUDA, capi.EBSD_EINVAL)
+        assert len(lib.ebsd_last_error(None)) > 0
+    rc = lib.ebsd_create(C.byref(h), 10_000)
+    assert rc in (capi.EBSD_ECUDA, capi.EBSD_EINVAL)
+
+
+def test_cli_help_and_template(built, tmp_path):
+    exe = capi.LIB_PATH.parent / "ctemebsd"
+    r = subprocess.run([str(exe), "-h"], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0 and "nmlfile" in r.stdout
+    r = subprocess.run([str(exe), "-t"], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0
+    tpl = tmp_path / "CTEMEBSD.template"
+    assert tpl.exists()
+    n = capi.read_namelist(tpl)  # the template parses with our own reader
+    assert n["numsx"] == 640 and n["scalingmode"] == "not"
+    r = subprocess.run([str(exe), str(tmp_path / "missing.nml")], capture_output=True,
+                       text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "cannot open" in r.stderr

@@ -6,7 +6,7 @@ import pytest
 
 from ctemsoft_gb300 import capi, synth
 from tests.conftest import workload_data
-from tests.parity import TOL_FP64, TOL_REF, cell_report, rel_errors
+from tests.parity import TOL_FP64, TOL_PIXEL_REF, TOL_REF, cell_report, rel_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -16,7 +16,7 @@ def _oracle():
     return O
 
 
-def _setup(wl, Emin=1, Emax=None, fp64=True, master=None, acc=None):
+def _setup(wl, Emin=1, Emax=None, fp64=True, master=None, acc=None, accurate=False):
     O = _oracle()
     sr, accum = workload_data(wl)
     if master is not None:
@@ -26,6 +26,7 @@ def _setup(wl, Emin=1, Emax=None, fp64=True, master=None, acc=None):
     Emax = wl.nEbins if Emax is None else Emax
     h = capi.Handle(0)
     h.set_option("weights_fp64", int(fp64))
+    h.set_option("lambert_accurate", int(accurate))
     h.set_master(sr)
     num_el = h.set_detector(wl.geometry(), accum, Emin, Emax)
     det = O.Detector(wl.geometry(), accum, Emin, Emax)
@@ -47,10 +48,15 @@ def test_tiny_parity(built, wl):
     gpu = h.forward(q, epi)
     p64 = det.patterns_f64(sr, q, pref)
     p32 = det.patterns_f32(sr, q, pref)
-    l2, mx = rel_errors(gpu, p64)
-    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64, (l2.max(), mx.max())
     l2, mx = rel_errors(gpu, p32)
     assert l2.max() <= TOL_REF and mx.max() <= TOL_REF, (l2.max(), mx.max())
+    # accurate Lambert arithmetic: within 1e-5 of FP64 pixel by pixel (these
+    # coarse 400 um detectors put many pixels near a pole, where the
+    # reference arithmetic itself is ~3e-4 off FP64)
+    h.set_option("lambert_accurate", 1)
+    acc_out = h.forward(q, epi)
+    l2, mx = rel_errors(acc_out, p64)
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64, (l2.max(), mx.max())
     h.close()
 
 
@@ -91,12 +97,16 @@ def test_c1_parity(built):
     p32 = det.patterns_f32(sr, q, pref, nthreads=O.max_threads())
     l2, mx = rel_errors(raw, p64)
     print("C1 vs FP64: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
-    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_PIXEL_REF
     l2, mx = rel_errors(raw, p32)
     assert l2.max() <= TOL_REF and mx.max() <= TOL_REF
     gam = h.forward(q, capi.epilogue(pref, scalingmode="gam", gammavalue=wl.gammavalue))
     ref = np.stack([O.epilogue_f64(p, 1, 2, wl.gammavalue) for p in p64])
     l2, mx = rel_errors(gam, ref)
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_PIXEL_REF
+    h.set_option("lambert_accurate", 1)
+    l2, mx = rel_errors(h.forward(q, capi.epilogue(pref)), p64)
+    print("C1 accurate vs FP64: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
     assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64
     h.close()
 
@@ -106,7 +116,7 @@ def test_c1_parity(built):
 def test_epilogue_binning(built, binning, mode):
     O = _oracle()
     wl = synth.tiny(seed=5, numsx=44, numsy=35, npx=30, nE=4, n_orient=5)
-    h, det, sr, num_el = _setup(wl)
+    h, det, sr, num_el = _setup(wl, accurate=True)
     q = wl.quaternions()
     pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
     out = h.forward(q, capi.epilogue(pref, binning=binning, scalingmode=mode, gammavalue=0.33))
@@ -145,7 +155,7 @@ def test_uniform_master(built):
 def test_identity_quaternion_is_detector_frame(built):
     """q = (1,0,0,0) gathers along the detector directions themselves."""
     wl = synth.tiny()
-    h, det, sr, num_el = _setup(wl)
+    h, det, sr, num_el = _setup(wl, accurate=True)
     q = np.array([[1, 0, 0, 0]], np.float32)
     out = h.forward(q, capi.epilogue(1.0))
     ref = det.patterns_f64(sr, q, 1.0)
@@ -176,7 +186,7 @@ def test_many_chunks_pageable(built):
     """More orientations than one device chunk: the double-buffered host
     path must keep every record in place."""
     wl = synth.tiny(numsx=640, numsy=480, npx=40, nE=5, n_orient=300)
-    h, det, sr, num_el = _setup(wl)
+    h, det, sr, num_el = _setup(wl, accurate=True)
     q = wl.quaternions()
     epi = capi.epilogue(1.0)
     out = h.forward(q, epi)
@@ -194,7 +204,7 @@ def test_many_chunks_pageable(built):
 
 def test_edge_cases(built):
     wl = synth.tiny()
-    h, det, sr, num_el = _setup(wl)
+    h, det, sr, num_el = _setup(wl, accurate=True)
     epi = capi.epilogue(1.0)
     # zero orientations is a no-op
     out = h.forward(np.zeros((0, 4), np.float32), epi)
@@ -253,7 +263,7 @@ def test_c2_subset_and_properties(built):
     p64 = det.patterns_f64(sr, q[sel], pref, nthreads=O.max_threads())
     l2, mx = rel_errors(out[sel], p64)
     print("C2 vs FP64: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
-    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_PIXEL_REF
     p32 = det.patterns_f32(sr, q[sel[:2]], pref, nthreads=O.max_threads())
     l2, mx = rel_errors(out[sel[:2]], p32)
     assert l2.max() <= TOL_REF and mx.max() <= TOL_REF
