@@ -49,6 +49,7 @@ def _args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--orient", type=int, default=10000)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--vjp-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -260,6 +261,13 @@ def run_ours(args):
     value = world * N * args.steps / (tot_ms / 1000.0)
     launch_ms = statistics.mean(step_ms)
 
+    # fused forward + adjoint: the normalised-dot-product loss and its
+    # gradient (3 rotation tangents + pattern centre) for every orientation
+    # against target patterns, one pass per pattern
+    fwd_vjp = None
+    if args.vjp_steps > 0:
+        fwd_vjp = _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, value)
+
     # end to end through the C ABI with host buffers
     del dout
     torch.cuda.empty_cache()
@@ -293,6 +301,7 @@ def run_ours(args):
                          "note": "gathered master bytes are served by L1/L2 (master is "
                                  "L2-resident), so frac can exceed 1"},
             "e2e": e2e,
+            "fwd_vjp": fwd_vjp,
             "gpu_launches": args.steps,
             "clocks": ck,
             "cpu_baseline": base,
@@ -302,6 +311,51 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, fwd_value):
+    import numpy as np
+    import torch
+
+    from ctemsoft_gb300 import capi, synth
+    N = len(q)
+    epi = capi.epilogue(pref)  # no gamma: the adjoint runs on linear patterns
+    # targets: patterns at orientations rotated by ~0.5 degree
+    rng = np.random.default_rng(11)
+    w = np.radians(rng.normal(0.0, 0.5, (N, 3)))
+    th = np.linalg.norm(w, axis=1, keepdims=True)
+    e = np.concatenate([np.cos(th / 2), np.sin(th / 2) * w / np.maximum(th, 1e-30)], axis=1)
+    qt = np.stack([e[:, 0] * q[:, 0] - (e[:, 1:] * q[:, 1:]).sum(1),
+                   e[:, 0] * q[:, 1] + e[:, 1] * q[:, 0] + e[:, 2] * q[:, 3] - e[:, 3] * q[:, 2],
+                   e[:, 0] * q[:, 2] - e[:, 1] * q[:, 3] + e[:, 2] * q[:, 0] + e[:, 3] * q[:, 1],
+                   e[:, 0] * q[:, 3] + e[:, 1] * q[:, 2] - e[:, 2] * q[:, 1] + e[:, 3] * q[:, 0]],
+                  axis=1).astype(np.float32)
+    dq = torch.from_numpy(q).to(dev)
+    h.forward(torch.from_numpy(qt).to(dev), epi, out=dout)  # targets in place
+    loss = torch.zeros(N, device=dev)
+    grad = torch.zeros((N, 6), device=dev)
+    for _ in range(max(1, args.warmup)):
+        h.vjp(dq, epi, dout, "ndp", loss=loss, grad=grad)
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.vjp_steps)]
+    for k in range(args.vjp_steps):
+        ev[k][0].record(stream)
+        h.vjp(dq, epi, dout, "ndp", loss=loss, grad=grad)
+        ev[k][1].record(stream)
+    barrier()
+    tot = sum(a.elapsed_time(b) for a, b in ev)
+    if world > 1:
+        t = torch.tensor([tot], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot = float(t.item())
+    v = world * N * args.vjp_steps / (tot / 1000.0)
+    lh = loss.cpu().numpy()
+    return {"value": v, "unit": UNIT, "ratio_to_forward": v / fwd_value,
+            "ms_per_step": tot / args.vjp_steps, "steps": args.vjp_steps,
+            "what": "loss 1 - normalised dot product + gradient w.r.t. 3 rotation tangents "
+                    "and (xpc, ypc, L), one fused pass per pattern",
+            "mean_loss": float(lh.mean()), "finite": bool(np.isfinite(lh).all())}
 
 
 def _e2e(h, q, epi, N, nx, ny, args, world, dev, barrier):

@@ -24,6 +24,8 @@ EBSD_EUNSUPPORTED = -7
 EBSD_ETIMEOUT = -8
 
 SCALING = {"not": 0, "lin": 1, "gam": 2}
+VJP_COTANGENT = 0
+VJP_NDP = 1
 
 
 class EBSDError(RuntimeError):
@@ -86,6 +88,7 @@ _SIGS = {
                                    C.POINTER(C.c_int32)]),
     "ebsd_forward": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P]),
     "ebsd_cells": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P, _P]),
+    "ebsd_vjp": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), C.c_int32, _P, _P, _P]),
     "ebsd_get_detector": (C.c_int, [_P, _P, _P, _P, _P]),
     "ebsd_run_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "ebsd_read_mc_file": (C.c_int, [C.c_char_p, C.POINTER(MCHeader), _P]),
@@ -230,6 +233,25 @@ class Handle:
             out = np.empty((n, ny, nx), dtype=np.float32)
         _check(lib().ebsd_forward(self._h, _ptr(quats), n, C.byref(epi), _ptr(out)), self._h)
         return out
+
+    def vjp(self, quats, epi: Epilogue, data, mode: str = "ndp", loss=None, grad=None):
+        """Adjoint of the pattern loop.  mode "ndp": data are target records,
+        returns (loss[n], grad[n, 6]) of 1 - normalised dot product; mode
+        "cot": data is the cotangent, returns (None, grad).  grad columns:
+        rotation tangent w0, w1, w2 [rad], xpc, ypc [px], L [um]."""
+        n = int(quats.shape[0])
+        if isinstance(quats, np.ndarray):
+            quats = np.ascontiguousarray(quats, dtype=np.float32)
+        if isinstance(data, np.ndarray):
+            data = np.ascontiguousarray(data, dtype=np.float32)
+        m = VJP_NDP if mode == "ndp" else VJP_COTANGENT
+        if grad is None:
+            grad = np.zeros((n, 6), np.float32)
+        if loss is None and m == VJP_NDP:
+            loss = np.zeros(n, np.float32)
+        _check(lib().ebsd_vjp(self._h, _ptr(quats), n, C.byref(epi), m, _ptr(data), _ptr(loss),
+                              _ptr(grad)), self._h)
+        return loss, grad
 
     def cells(self, quats: np.ndarray):
         q = np.ascontiguousarray(quats, dtype=np.float32)

@@ -41,12 +41,17 @@ struct ebsd_handle {
     int32_t num_el = 0;
     float4* d_rg = nullptr;
     float4* d_W = nullptr;
+    float4* d_drg = nullptr;   // [3][P] d rg / d(xpc, ypc, L)
+    float4* d_dW = nullptr;    // [3][NV][P] d W / d(xpc, ypc, L)
     int P = 0;
+    int nsx = 0, nsy = 0;
 
     // per-call buffers
     DeviceBuf quats[2];
     DeviceBuf outb[2];
     DeviceBuf tmp;
+    DeviceBuf vjp_partial;     // per-CTA partial sums of the adjoint
+    DeviceBuf vjp_io;          // device copies of host quats / data / outputs
     float* pinned[2] = {nullptr, nullptr};
     size_t pinned_bytes = 0;
     cudaEvent_t ev_comp[2] = {nullptr, nullptr};
@@ -277,6 +282,10 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
     cudaFree(h->d_master_il);
     cudaFree(h->d_rg);
     cudaFree(h->d_W);
+    cudaFree(h->d_drg);
+    cudaFree(h->d_dW);
+    cudaFree(h->vjp_partial.ptr);
+    cudaFree(h->vjp_io.ptr);
     for (int i = 0; i < 2; ++i) {
         cudaFree(h->quats[i].ptr);
         cudaFree(h->outb[i].ptr);
@@ -312,6 +321,15 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
         h->weights_fp64 = value != 0;
         if (h->have_detector)
             return set_err(h, EBSD_ESTATE, "weights_fp64 applies at the next ebsd_set_detector");
+    } else if (k == "strict_order") {
+        h->cfg.strict = value != 0;
+    } else if (k == "l2_persist") {
+        if (!value) {
+            h->cfg.persist_base = nullptr;
+            h->cfg.persist_bytes = 0;
+        } else if (!h->cfg.persist_base) {
+            return set_err(h, EBSD_ESTATE, "l2_persist: no persisting window on this device/detector");
+        }
     } else if (k == "lambert_accurate") {
         h->lambert_accurate = value != 0;
     } else if (k == "tile_y") {
@@ -414,10 +432,16 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
     const int NV = (nsel + 3) / 4;
     cudaFree(h->d_rg);
     cudaFree(h->d_W);
+    cudaFree(h->d_drg);
+    cudaFree(h->d_dW);
     h->d_rg = nullptr;
     h->d_W = nullptr;
+    h->d_drg = nullptr;
+    h->d_dW = nullptr;
     CK(h, cudaMalloc(&h->d_rg, sizeof(float4) * (size_t)P), "cudaMalloc rg");
     CK(h, cudaMalloc(&h->d_W, sizeof(float4) * (size_t)P * NV), "cudaMalloc W");
+    CK(h, cudaMalloc(&h->d_drg, sizeof(float4) * (size_t)P * 3), "cudaMalloc drg");
+    CK(h, cudaMalloc(&h->d_dW, sizeof(float4) * (size_t)P * 3 * NV), "cudaMalloc dW");
 
     // master re-layout for this window
     if (h->il_e0 != Emin - 1 || h->il_nsel != nsel) {
@@ -447,6 +471,9 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
     cudaError_t e = launch_weights(h->d_rg, P, (const int32_t*)h->tmp.ptr, numEbins, nsx, nsy,
                                    sclmc, host::lambert_spi2_f(), Emin - 1, nsel, NV,
                                    h->weights_fp64, *g, h->d_W, d_wref, s);
+    if (e == cudaSuccess)
+        e = launch_geom_derivs(*g, (const int32_t*)h->tmp.ptr, numEbins, nsx, nsy, Emin - 1, nsel,
+                               NV, h->d_drg, h->d_dW, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     // num_el reuses the start of the histogram buffer, after the weights ran
     float* d_sum = (float*)h->tmp.ptr;
@@ -465,11 +492,22 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
     h->nsel = nsel;
     h->NV = NV;
     h->P = P;
+    h->nsx = nsx;
+    h->nsy = nsy;
 
-    // keep the master resident in L2 for the pattern kernels
-    if (h->max_persist > 0) {
-        size_t want = std::min(h->il_bytes, (size_t)h->max_persist);
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want);
+    // keep the master resident in L2 for the pattern kernels: a persisting
+    // carve-out (a limit of this process's context) and an access-policy
+    // window attached to every pattern-kernel launch
+    h->cfg.persist_base = nullptr;
+    h->cfg.persist_bytes = 0;
+    if (h->max_persist > 0 && h->max_window > 0) {
+        const size_t carve = std::min(h->il_bytes, (size_t)h->max_persist);
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, carve) == cudaSuccess) {
+            const size_t win = std::min(h->il_bytes, (size_t)h->max_window);
+            h->cfg.persist_base = h->d_master_il;
+            h->cfg.persist_bytes = win;
+            h->cfg.persist_hit_ratio = std::min(1.0f, (float)carve / (float)win);
+        }
         cudaGetLastError();
     }
     h->have_detector = true;
@@ -599,6 +637,97 @@ extern "C" int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const
     }
     // the caller's stream sees completed work
     CK(h, cudaStreamSynchronize(s), "forward");
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
+                        int32_t mode, const float* data, float* loss, float* grad)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n < 0) return set_err(h, EBSD_EINVAL, "negative orientation count");
+    if (n == 0) return EBSD_OK;
+    if (!quats || !e || !data || !grad) return set_err(h, EBSD_EINVAL, "ebsd_vjp: null argument");
+    if (mode != EBSD_VJP_COTANGENT && mode != EBSD_VJP_NDP)
+        return set_err(h, EBSD_EINVAL, "ebsd_vjp: unknown mode %d", mode);
+    if (e->scalingmode == EBSD_SCALING_GAM || e->poisson)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_vjp: gamma and noise epilogues have no adjoint");
+    if (h->NV > 8)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_vjp: at most 32 energy bins (window has %d)",
+                       h->nsel);
+    rc = activate(h);
+    if (rc) return rc;
+    FwdParams p;
+    rc = fill_params(h, e, p);
+    if (rc) return rc;
+    VjpParams vp;
+    memset(&vp, 0, sizeof vp);
+    vp.drg = h->d_drg;
+    vp.dW = h->d_dW;
+    vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
+    vp.opc = 2;
+    const int tile_y = 8;
+    if (vp.binning > tile_y)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_vjp: binning %d exceeds the tile", vp.binning);
+    const int K = mode == EBSD_VJP_NDP ? 15 : 6;
+    const int ntiles = vjp_tiles(p, tile_y);
+    const size_t rec = (size_t)p.out_nx * p.out_ny;
+    cudaStream_t s = h->stream;
+    const bool qdev = ptr_kind(quats) == kDevice, ddev = ptr_kind(data) == kDevice;
+    const bool gdev = ptr_kind(grad) == kDevice;
+    const bool ldev = loss ? ptr_kind(loss) == kDevice : true;
+    if (!qdev) {
+        rc = check_quats_host(h, quats, n);
+        if (rc) return rc;
+    }
+    // chunk so that partials and staged records stay bounded
+    const size_t budget = size_t(256) << 20;
+    const size_t per_o = (size_t)ntiles * K * sizeof(float) + (ddev ? 0 : rec * sizeof(float));
+    int64_t chunk = (int64_t)std::max<size_t>(1, budget / per_o);
+    chunk = std::min<int64_t>(chunk, n);
+    rc = ensure(h, h->vjp_partial, (size_t)chunk * ntiles * K * sizeof(float), "adjoint partials");
+    if (rc) return rc;
+    // device staging: quats (16 B/o) + data + loss + grad (28 B/o)
+    const size_t io_bytes = (size_t)chunk * (16 + 28) + (ddev ? 0 : (size_t)chunk * rec * 4) + 256;
+    rc = ensure(h, h->vjp_io, io_bytes, "adjoint staging");
+    if (rc) return rc;
+    char* io = (char*)h->vjp_io.ptr;
+    float4* dq = (float4*)io;
+    float* dgrad = (float*)(io + (size_t)chunk * 16);
+    float* dloss = dgrad + (size_t)chunk * 6;
+    float* ddata = dloss + chunk;
+    for (int64_t o0 = 0; o0 < n; o0 += chunk) {
+        const int64_t m = std::min<int64_t>(chunk, n - o0);
+        p.n = m;
+        if (qdev) {
+            p.quats = (const float4*)quats + o0;
+        } else {
+            CK(h, cudaMemcpyAsync(dq, quats + 4 * o0, sizeof(float4) * m, cudaMemcpyHostToDevice, s),
+               "quaternion upload");
+            p.quats = dq;
+        }
+        if (ddev) {
+            vp.data = data + (size_t)o0 * rec;
+        } else {
+            CK(h, cudaMemcpyAsync(ddata, data + (size_t)o0 * rec, sizeof(float) * m * rec,
+                                  cudaMemcpyHostToDevice, s),
+               "record upload");
+            vp.data = ddata;
+        }
+        vp.partial = (float*)h->vjp_partial.ptr;
+        vp.grad = gdev ? grad + 6 * o0 : dgrad;
+        vp.loss = loss ? (ldev ? loss + o0 : dloss) : nullptr;
+        cudaError_t ce = launch_vjp(p, vp, h->NV, mode, tile_y, s);
+        if (ce != cudaSuccess) return cuda_err(h, ce, "adjoint kernel launch");
+        if (!gdev)
+            CK(h, cudaMemcpyAsync(grad + 6 * o0, dgrad, sizeof(float) * 6 * m,
+                                  cudaMemcpyDeviceToHost, s),
+               "gradient copy");
+        if (loss && !ldev)
+            CK(h, cudaMemcpyAsync(loss + o0, dloss, sizeof(float) * m, cudaMemcpyDeviceToHost, s),
+               "loss copy");
+        if (!qdev || !ddev || !gdev || !ldev) CK(h, cudaStreamSynchronize(s), "adjoint");
+    }
     return EBSD_OK;
 }
 

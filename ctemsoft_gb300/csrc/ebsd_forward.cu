@@ -24,8 +24,13 @@ namespace {
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
 // Sum over the window of W(k) * bilinear(sr(.,.,k)), the loop body of
-// CTEMEBSD.f90:600-604 in its own evaluation order.
-template <int NV>
+// CTEMEBSD.f90:600-604.  STRICT evaluates it in the reference's own order
+// (((s00*dxm)*dym + (s10*dx)*dym + ...) per bin, accumulated bin by bin,
+// no fused operations).  Otherwise the same sum is taken as four dot
+// products of the weights with the four corner vectors, each accumulated
+// with fused multiply-adds, then combined with the bilinear corner weights:
+// about a third of the arithmetic, and no less accurate.
+template <int NV, bool STRICT>
 __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master, int gx,
                                               int ix0, int iy0, int ix1, int iy1, float dx,
                                               float dy, const float4 (&w)[NV])
@@ -35,16 +40,29 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
     const float4* m10 = master + ((int64_t)iy0 * gx + ix1) * NV;
     const float4* m01 = master + ((int64_t)iy1 * gx + ix0) * NV;
     const float4* m11 = master + ((int64_t)iy1 * gx + ix1) * NV;
-    float acc = 0.0f;
+    if (STRICT) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            const float4 a = ldg4(m00 + c), b = ldg4(m10 + c), e = ldg4(m01 + c),
+                         f = ldg4(m11 + c);
+            acc = acc + w[c].x * (a.x * dxm * dym + b.x * dx * dym + e.x * dxm * dy + f.x * dx * dy);
+            acc = acc + w[c].y * (a.y * dxm * dym + b.y * dx * dym + e.y * dxm * dy + f.y * dx * dy);
+            acc = acc + w[c].z * (a.z * dxm * dym + b.z * dx * dym + e.z * dxm * dy + f.z * dx * dy);
+            acc = acc + w[c].w * (a.w * dxm * dym + b.w * dx * dym + e.w * dxm * dy + f.w * dx * dy);
+        }
+        return acc;
+    }
+    float c00 = 0.0f, c10 = 0.0f, c01 = 0.0f, c11 = 0.0f;
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
         const float4 a = ldg4(m00 + c), b = ldg4(m10 + c), e = ldg4(m01 + c), f = ldg4(m11 + c);
-        acc = acc + w[c].x * (a.x * dxm * dym + b.x * dx * dym + e.x * dxm * dy + f.x * dx * dy);
-        acc = acc + w[c].y * (a.y * dxm * dym + b.y * dx * dym + e.y * dxm * dy + f.y * dx * dy);
-        acc = acc + w[c].z * (a.z * dxm * dym + b.z * dx * dym + e.z * dxm * dy + f.z * dx * dy);
-        acc = acc + w[c].w * (a.w * dxm * dym + b.w * dx * dym + e.w * dxm * dy + f.w * dx * dy);
+        c00 = fmaf(w[c].x, a.x, fmaf(w[c].y, a.y, fmaf(w[c].z, a.z, fmaf(w[c].w, a.w, c00))));
+        c10 = fmaf(w[c].x, b.x, fmaf(w[c].y, b.y, fmaf(w[c].z, b.z, fmaf(w[c].w, b.w, c10))));
+        c01 = fmaf(w[c].x, e.x, fmaf(w[c].y, e.y, fmaf(w[c].z, e.z, fmaf(w[c].w, e.w, c01))));
+        c11 = fmaf(w[c].x, f.x, fmaf(w[c].y, f.y, fmaf(w[c].z, f.z, fmaf(w[c].w, f.w, c11))));
     }
-    return acc;
+    return fmaf(c00, dxm * dym, fmaf(c10, dx * dym, fmaf(c01, dxm * dy, c11 * (dx * dy))));
 }
 
 // Rotated, projected and scaled Lambert coordinates of one pixel for one
@@ -62,7 +80,7 @@ __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, fl
     ixy1 = scl * Y;
 }
 
-template <int NV>
+template <int NV, bool STRICT>
 __global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y, int tiles_x,
                                                  int ntiles, int opc)
 {
@@ -101,7 +119,8 @@ __global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y
             const int ix0 = lambert_cell(ixy0, prm.npx, dx, nix);
             const int iy0 = lambert_cell(ixy1, prm.npy, dy, niy);
             const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
-            const float acc = gather_pixel<NV>(prm.master, prm.gx, ix0, iy0, ix1, iy1, dx, dy, w);
+            const float acc =
+                gather_pixel<NV, STRICT>(prm.master, prm.gx, ix0, iy0, ix1, iy1, dx, dy, w);
             val = (float)(prm.prefactor * (double)acc);                      // :608
         }
         if (!binned) {
@@ -148,8 +167,8 @@ __global__ void k_cells(const FwdParams prm)
     prm.ixy1[idx] = ixy1;
 }
 
-template <int NV>
-cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
+template <int NV, bool STRICT>
+cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
     const int tile_y = cfg.tile_y;
     const int tiles_x = (p.numsx + kTileX - 1) / kTileX;
@@ -159,10 +178,20 @@ cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
     const int64_t oblocks = (p.n + opc - 1) / opc;
     const int64_t blocks = oblocks * ntiles;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    const size_t smem = sizeof(float) * 33 * tile_y;
-    k_forward<NV><<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, tile_y, tiles_x, ntiles,
-                                                                   opc);
-    return cudaGetLastError();
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)blocks);
+    lc.blockDim = dim3(kTileX * tile_y);
+    lc.dynamicSmemBytes = sizeof(float) * 33 * tile_y;
+    lc.stream = s;
+    cudaLaunchAttribute attr[1];
+    set_persist_attr(cfg, attr, lc);
+    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT>, p, tile_y, tiles_x, ntiles, opc);
+}
+
+template <int NV>
+cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
+{
+    return cfg.strict ? launch_nv2<NV, true>(p, cfg, s) : launch_nv2<NV, false>(p, cfg, s);
 }
 
 }  // namespace

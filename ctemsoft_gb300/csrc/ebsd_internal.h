@@ -47,11 +47,45 @@ struct FwdParams {
     float* ixy1;
 };
 
+// Adjoint-only inputs and outputs (ebsd_vjp.cu).  Pointers are offset to
+// the current chunk of orientations by the caller.
+struct VjpParams {
+    const float4* drg;   // [3][P] d rg / d(xpc, ypc, L)
+    const float4* dW;    // [3][NV][P] d W / d(xpc, ypc, L)
+    const float* data;   // [n][out_ny][out_nx] cotangent or targets
+    float* partial;      // scratch [n][ntiles][K]
+    float* loss;         // [n] or null
+    float* grad;         // [n][6]
+    int binning;         // 1 for 'not'
+    int opc;             // orientations per CTA
+};
+
 // Launch configuration picked by the tuner or by default.
 struct LaunchCfg {
     int tile_y = 8;        // CTA is 32 x tile_y pixels
     int orient_per_cta = 4;
+    bool strict = false;   // reference summation order in the gather
+    // L2 access-policy window kept persisting for the master pattern
+    const void* persist_base = nullptr;
+    size_t persist_bytes = 0;
+    float persist_hit_ratio = 0.0f;
 };
+
+// Attach the master's persisting-L2 window to a launch (no-op when unset).
+inline void set_persist_attr(const LaunchCfg& cfg, cudaLaunchAttribute* attr,
+                             cudaLaunchConfig_t& lc)
+{
+    lc.attrs = attr;
+    lc.numAttrs = 0;
+    if (!cfg.persist_base || cfg.persist_bytes == 0) return;
+    attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(cfg.persist_base);
+    attr[0].val.accessPolicyWindow.num_bytes = cfg.persist_bytes;
+    attr[0].val.accessPolicyWindow.hitRatio = cfg.persist_hit_ratio;
+    attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    lc.numAttrs = 1;
+}
 
 // Setup-stage kernels (ebsd_setup.cu).
 cudaError_t launch_master_relayout(const float* raw, int npx, int npy, int nE, int numset,
@@ -63,6 +97,15 @@ cudaError_t launch_weights(const float4* rg, int P, const int32_t* accum_e, int 
                            const ebsd_geometry& g, float4* W, float4* Wref, cudaStream_t s);
 cudaError_t launch_num_el(const float4* W, int P, int nsel, int NV, float* sum_out,
                           cudaStream_t s);
+
+cudaError_t launch_geom_derivs(const ebsd_geometry& g, const int32_t* accum_e, int nE, int nsx,
+                               int nsy, int e0, int nsel, int NV, float4* drg, float4* dW,
+                               cudaStream_t s);
+
+// Adjoint (ebsd_vjp.cu).
+int vjp_tiles(const FwdParams& p, int tile_y);
+cudaError_t launch_vjp(const FwdParams& p, const VjpParams& vp, int NV, int mode, int tile_y,
+                       cudaStream_t s);
 
 // Pattern kernels (ebsd_forward.cu).
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s);

@@ -251,3 +251,128 @@ cudaError_t launch_num_el(const float4* W, int P, int nsel, int NV, float* sum_o
 }
 
 }  // namespace ebsd
+
+namespace ebsd {
+
+// Derivatives of the detector quantities with respect to the pattern centre
+// (xpc, ypc in pixels; L in microns), evaluated in binary64:
+//   drg[a][p] = d rg(p) / d theta_a, rg = v/|v| with v the unnormalised
+//               direction of CTEMEBSD.f90:434-442;
+//   dW[a][c][p] = d W(p) / d theta_a for the window bins (float4 planes),
+//               through the Lambert point of rg on the MC grid (:486-506).
+// The cell indices are locally constant, so only the bilinear fractions
+// carry derivatives.
+__global__ void k_geom_derivs(WeightsGeom gd, const int32_t* __restrict__ acc, int nE, int nsx,
+                              int nsy, int e0, int nsel, int NV, float4* __restrict__ drg,
+                              float4* __restrict__ dW, int P)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const int i = p % gd.numsx, j = p / gd.numsx;
+    const double sxp = -(gd.xpc - (1.0 - gd.numsx) * 0.5 - i) * gd.delta;
+    const double syp = (gd.ypc - (1.0 - gd.numsy) * 0.5 - j) * gd.delta;
+    const double v[3] = {gd.ca * syp + gd.L * gd.sa, sxp, -gd.sa * syp + gd.L * gd.ca};
+    const double nv = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    const double r[3] = {v[0] / nv, v[1] / nv, v[2] / nv};
+    const double dv[3][3] = {{0.0, -gd.delta, 0.0},
+                             {gd.ca * gd.delta, 0.0, -gd.sa * gd.delta},
+                             {gd.sa, 0.0, gd.ca}};
+    double dr[3][3];
+    for (int a = 0; a < 3; ++a) {
+        const double pr = r[0] * dv[a][0] + r[1] * dv[a][1] + r[2] * dv[a][2];
+        for (int c = 0; c < 3; ++c) dr[a][c] = (dv[a][c] - pr * r[c]) / nv;
+        drg[(int64_t)a * P + p] = make_float4((float)dr[a][0], (float)dr[a][1], (float)dr[a][2],
+                                              0.0f);
+    }
+    // MC Lambert point and its Jacobian (Lambert.f90:452-483 differentiated)
+    double x = r[0], y = r[1], z = r[2], sm = 1.0;
+    if (z < 0.0) {
+        x = -x;
+        y = -y;
+        z = -z;
+        sm = -1.0;
+    }
+    const double spi2 = 0.88622692545275801365;
+    double LX = 0.0, LY = 0.0, dX[3] = {0, 0, 0}, dY[3] = {0, 0, 0};
+    const double rxy = x * x + y * y;
+    if (fabs(z) != 1.0 && rxy > 0.0) {
+        const double rho = sqrt(2.0 * (1.0 - z));
+        if (fabs(y) <= fabs(x)) {
+            const double sg = copysign(1.0, x), a = atan(y / x);
+            LX = sg * rho * spi2;
+            LY = sg * rho * a / spi2;
+            dX[2] = -sg * spi2 / rho;
+            dY[0] = sg * rho / spi2 * (-y / rxy);
+            dY[1] = sg * rho / spi2 * (x / rxy);
+            dY[2] = -sg * a / (spi2 * rho);
+        } else {
+            const double sg = copysign(1.0, y), b = atan(x / y);
+            LX = sg * rho * b / spi2;
+            LY = sg * rho * spi2;
+            dX[0] = sg * rho / spi2 * (y / rxy);
+            dX[1] = sg * rho / spi2 * (-x / rxy);
+            dX[2] = -sg * b / (spi2 * rho);
+            dY[2] = -sg * spi2 / rho;
+        }
+    }
+    const double scl = (double)nsx / 1.25331413731550025121;
+    double Dx, Dy;
+    int jx0, jy0;
+    cell_f64(scl * LY, nsx, Dx, jx0);
+    cell_f64(-(scl * LX), nsy, Dy, jy0);
+    const int jx1 = min(jx0 + 1, 2 * nsx), jy1 = min(jy0 + 1, 2 * nsy);
+    const double Dxm = 1.0 - Dx, Dym = 1.0 - Dy;
+    double di0[3], di1[3];
+    for (int a = 0; a < 3; ++a) {
+        di0[a] = scl * sm * (dY[0] * dr[a][0] + dY[1] * dr[a][1] + dY[2] * dr[a][2]);
+        di1[a] = -scl * sm * (dX[0] * dr[a][0] + dX[1] * dr[a][1] + dX[2] * dr[a][2]);
+    }
+    const int64_t gxm = 2 * nsx + 1;
+    const int32_t* a00 = acc + ((int64_t)jy0 * gxm + jx0) * nE + e0;
+    const int32_t* a10 = acc + ((int64_t)jy0 * gxm + jx1) * nE + e0;
+    const int32_t* a01 = acc + ((int64_t)jy1 * gxm + jx0) * nE + e0;
+    const int32_t* a11 = acc + ((int64_t)jy1 * gxm + jx1) * nE + e0;
+    for (int a = 0; a < 3; ++a) {
+        for (int c = 0; c < NV; ++c) {
+            float u[4];
+            for (int t = 0; t < 4; ++t) {
+                const int k = 4 * c + t;
+                double g = 0.0;
+                if (k < nsel) {
+                    const double g0 = 0.25 * ((double)(a10[k] - a00[k]) * Dym +
+                                              (double)(a11[k] - a01[k]) * Dy);
+                    const double g1 = 0.25 * ((double)(a01[k] - a00[k]) * Dxm +
+                                              (double)(a11[k] - a10[k]) * Dx);
+                    g = g0 * di0[a] + g1 * di1[a];
+                }
+                u[t] = (float)g;
+            }
+            dW[((int64_t)a * NV + c) * P + p] = make_float4(u[0], u[1], u[2], u[3]);
+        }
+    }
+}
+
+cudaError_t launch_geom_derivs(const ebsd_geometry& g, const int32_t* accum_e, int nE, int nsx,
+                               int nsy, int e0, int nsel, int NV, float4* drg, float4* dW,
+                               cudaStream_t s)
+{
+    WeightsGeom gd;
+    const double dtor = (double)0.0174533f;
+    const double alp =
+        0.5 * 3.141592653589793238 - ((double)(float)g.sig - (double)g.thetac) * dtor;
+    gd.L = g.L;
+    gd.delta = g.delta;
+    gd.xpc = g.xpc;
+    gd.ypc = g.ypc;
+    gd.ca = cos(alp);
+    gd.sa = sin(alp);
+    gd.numsx = g.numsx;
+    gd.numsy = g.numsy;
+    const int P = g.numsx * g.numsy;
+    const int bs = 128;
+    k_geom_derivs<<<(P + bs - 1) / bs, bs, 0, s>>>(gd, accum_e, nE, nsx, nsy, e0, nsel, NV, drg,
+                                                   dW, P);
+    return cudaGetLastError();
+}
+
+}  // namespace ebsd

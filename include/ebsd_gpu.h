@@ -132,6 +132,28 @@ int ebsd_output_dims(const ebsd_handle* h, const ebsd_epilogue* e, int32_t* nx, 
 int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
                  float* out);
 
+/* Adjoint modes of ebsd_vjp. */
+#define EBSD_VJP_COTANGENT 0 /* data = cotangent on the output records */
+#define EBSD_VJP_NDP 1       /* data = target records; loss = 1 - normalised dot product */
+
+/* Vector-Jacobian product of the pattern loop (no reference counterpart:
+ * the reference has no derivatives; it differentiates CTEMEBSD.f90:577-608
+ * and the detector set-up :416-510).  Parameters per orientation o, in
+ * grad[o*6 + 0..5]: the left rotation tangent (w0, w1, w2) in radians,
+ * q(w) = exp(w) (x) q with exp(w) = (cos(|w|/2), sin(|w|/2) w/|w|), and the
+ * pattern centre xpc, ypc [pixels] and L [microns] (the gradient of this
+ * orientation's output with respect to the detector's shared pattern
+ * centre).  The forward gather is recomputed, not stored.
+ *   EBSD_VJP_COTANGENT: grad = sum over record pixels of cot * dOut/dparam;
+ *                       loss may be NULL.
+ *   EBSD_VJP_NDP:       loss[o] = 1 - <Out,T>/(|Out||T|) against the target
+ *                       record T, and grad = dloss/dparam, in one pass.
+ * data holds n records of the size ebsd_output_dims gives; the epilogue
+ * may bin ('lin') but not apply gamma or noise.  Pointers may be host or
+ * device memory. */
+int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e, int32_t mode,
+             const float* data, float* loss, float* grad);
+
 /* Lambert cells of the loop (CTEMEBSD.f90:584-598) for n quaternions:
  * nix/niy (grid indices in -npx..npx) and the scaled Lambert coordinates
  * ixy0/ixy1, each [n][numsy][numsx].  Host or device pointers.  For parity

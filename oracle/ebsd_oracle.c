@@ -293,19 +293,19 @@ void oracle_detector_f32(const oracle_geometry* g, float* rgx, float* rgy, float
     free(scin_y);
 }
 
-void oracle_detector_f64(const oracle_geometry* g, double* rgx, double* rgy, double* rgz)
+void oracle_detector_f64(const oracle_geometry_d* g, double* rgx, double* rgy, double* rgz)
 {
     const int nx = g->numsx, ny = g->numsy;
     const double dtor = (double)DTOR_F;
     const double L = g->L, delta = g->delta;
-    double alp = 0.5 * PI_D - ((double)(float)g->sig - (double)g->thetac) * dtor;
+    double alp = 0.5 * PI_D - (g->sig - g->thetac) * dtor;
     double ca = cos(alp), sa = sin(alp);
     for (int j = 0; j < ny; ++j) {
-        double sy = ((double)g->ypc - (1.0 - ny) * 0.5 - j) * delta;
+        double sy = (g->ypc - (1.0 - ny) * 0.5 - j) * delta;
         double Ls = ca * sy + L * sa;
         double Lc = -sa * sy + L * ca;
         for (int i = 0; i < nx; ++i) {
-            double sx = -((double)g->xpc - (1.0 - nx) * 0.5 - i) * delta;
+            double sx = -(g->xpc - (1.0 - nx) * 0.5 - i) * delta;
             double rhos = 1.0 / sqrt(L * L + sy * sy + sx * sx);
             double x = Ls * rhos, y = sx * rhos, z = Lc * rhos;
             double n = sqrt(x * x + y * y + z * z);
@@ -373,7 +373,7 @@ int32_t oracle_mc_weights_f32(const oracle_geometry* g, const float* rgx, const 
 
 /* FP64 re-evaluation of the weights (same clamping, bins outside zero).
  * Returns the binary64 sum of W. */
-double oracle_mc_weights_f64(const oracle_geometry* g, const double* rgx, const double* rgy,
+double oracle_mc_weights_f64(const oracle_geometry_d* g, const double* rgx, const double* rgy,
                              const double* rgz, const int32_t* accum_e, int nE, int nsx,
                              int nsy, int Emin, int Emax, double* W)
 {
@@ -541,10 +541,10 @@ void oracle_patterns_f32(const oracle_geometry* g, const float* rgx, const float
 }
 
 /* FP64 re-evaluation of the loop: binary64 throughout, with the inputs
- * (quaternions, master, geometry) taken at their stored float values. */
-void oracle_patterns_f64(const oracle_geometry* g, const double* rgx, const double* rgy,
+ * (master at its stored float values; geometry and quaternions in binary64). */
+void oracle_patterns_f64(const oracle_geometry_d* g, const double* rgx, const double* rgy,
                          const double* rgz, const double* W, int nE, int Emin, int Emax,
-                         const float* sr, int npx, int npy, const float* quats, int64_t N,
+                         const float* sr, int npx, int npy, const double* quats, int64_t N,
                          double prefactor, double* out, int nthreads)
 {
     const int nx = g->numsx, ny = g->numsy;

@@ -20,6 +20,15 @@ typedef struct {
     double sig; /* MC file sample tilt, degrees (CTEMMC.f90:272) */
 } oracle_geometry;
 
+/* The same geometry in binary64, for the FP64 re-evaluation and its
+ * derivatives (finite differences need steps finer than float spacing). */
+typedef struct {
+    double L, thetac, delta;
+    int32_t numsx, numsy;
+    double xpc, ypc;
+    double sig;
+} oracle_geometry_d;
+
 int oracle_lambert_inverse_f32(const float xyz[3], float res[2]);
 int oracle_lambert_inverse_f64(const double xyz[3], double res[2]);
 int oracle_lambert_forward_f64(const double xy[2], double res[3]);
@@ -30,12 +39,12 @@ void oracle_angles_to_quats_f32(const float* rows, int64_t n, int mode, int hkl,
                                 const float axisangle[4], float* quats);
 
 void oracle_detector_f32(const oracle_geometry* g, float* rgx, float* rgy, float* rgz);
-void oracle_detector_f64(const oracle_geometry* g, double* rgx, double* rgy, double* rgz);
+void oracle_detector_f64(const oracle_geometry_d* g, double* rgx, double* rgy, double* rgz);
 
 int32_t oracle_mc_weights_f32(const oracle_geometry* g, const float* rgx, const float* rgy,
                               const float* rgz, const int32_t* accum_e, int nE, int nsx,
                               int nsy, int Emin, int Emax, float* W);
-double oracle_mc_weights_f64(const oracle_geometry* g, const double* rgx, const double* rgy,
+double oracle_mc_weights_f64(const oracle_geometry_d* g, const double* rgx, const double* rgy,
                              const double* rgz, const int32_t* accum_e, int nE, int nsx,
                              int nsy, int Emin, int Emax, double* W);
 double oracle_prefactor(double beamcurrent, double dwelltime, int32_t num_el);
@@ -50,10 +59,21 @@ void oracle_patterns_f32(const oracle_geometry* g, const float* rgx, const float
                          const float* rgz, const float* W, int nE, int Emin, int Emax,
                          const float* sr, int npx, int npy, const float* quats, int64_t N,
                          double prefactor, float* out, int nthreads);
-void oracle_patterns_f64(const oracle_geometry* g, const double* rgx, const double* rgy,
+void oracle_patterns_f64(const oracle_geometry_d* g, const double* rgx, const double* rgy,
                          const double* rgz, const double* W, int nE, int Emin, int Emax,
-                         const float* sr, int npx, int npy, const float* quats, int64_t N,
+                         const float* sr, int npx, int npy, const double* quats, int64_t N,
                          double prefactor, double* out, int nthreads);
+
+/* Analytic FP64 derivatives (ebsd_oracle_grad.c).  Parameters per pattern:
+ * left rotation tangent (w0,w1,w2), q(w) = exp(w) (x) q, and the pattern
+ * centre (xpc, ypc, L).  mode 0: cotangent -- grad[n] = sum_B cot[n][B] *
+ * dO[n][B]/dphi; mode 1: normalised-dot-product loss against targets
+ * (data = targets), loss[n] = 1 - <O,T>/(|O||T|).  O is the output record
+ * after prefactor and binning ('lin' for binning > 1). */
+void oracle_vjp_f64(const oracle_geometry_d* g, const int32_t* accum_e, int nE, int nsx, int nsy,
+                    int Emin, int Emax, const float* sr, int npx, int npy, const double* quats,
+                    int64_t N, double prefactor, int binning, int mode, const float* data,
+                    double* loss, double* grad, int nthreads);
 void oracle_epilogue_f32(const float* pat, int numsx, int numsy, int binning, int mode,
                          float gammavalue, float* out);
 void oracle_epilogue_f64(const double* pat, int numsx, int numsy, int binning, int mode,

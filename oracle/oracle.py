@@ -29,6 +29,12 @@ class Geometry(C.Structure):
                 ("ypc", C.c_float), ("sig", C.c_double)]
 
 
+class GeometryD(C.Structure):
+    _fields_ = [("L", C.c_double), ("thetac", C.c_double), ("delta", C.c_double),
+                ("numsx", C.c_int32), ("numsy", C.c_int32), ("xpc", C.c_double),
+                ("ypc", C.c_double), ("sig", C.c_double)]
+
+
 _P = C.c_void_p
 _SIGS = {
     "oracle_lambert_inverse_f32": (C.c_int, [_P, _P]),
@@ -39,10 +45,10 @@ _SIGS = {
     "oracle_ax2qu_f32": (None, [_P, _P]),
     "oracle_angles_to_quats_f32": (None, [_P, C.c_int64, C.c_int, C.c_int, _P, _P]),
     "oracle_detector_f32": (None, [C.POINTER(Geometry), _P, _P, _P]),
-    "oracle_detector_f64": (None, [C.POINTER(Geometry), _P, _P, _P]),
+    "oracle_detector_f64": (None, [C.POINTER(GeometryD), _P, _P, _P]),
     "oracle_mc_weights_f32": (C.c_int32, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int, C.c_int,
                                           C.c_int, C.c_int, C.c_int, _P]),
-    "oracle_mc_weights_f64": (C.c_double, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int,
+    "oracle_mc_weights_f64": (C.c_double, [C.POINTER(GeometryD), _P, _P, _P, _P, C.c_int,
                                            C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "oracle_prefactor": (C.c_double, [C.c_double, C.c_double, C.c_int32]),
     "oracle_energy_window": (None, [C.c_float, C.c_float, C.c_double, C.c_double, C.c_int,
@@ -53,9 +59,12 @@ _SIGS = {
     "oracle_patterns_f32": (None, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int, C.c_int,
                                    C.c_int, _P, C.c_int, C.c_int, _P, C.c_int64, C.c_double, _P,
                                    C.c_int]),
-    "oracle_patterns_f64": (None, [C.POINTER(Geometry), _P, _P, _P, _P, C.c_int, C.c_int,
+    "oracle_patterns_f64": (None, [C.POINTER(GeometryD), _P, _P, _P, _P, C.c_int, C.c_int,
                                    C.c_int, _P, C.c_int, C.c_int, _P, C.c_int64, C.c_double, _P,
                                    C.c_int]),
+    "oracle_vjp_f64": (None, [C.POINTER(GeometryD), _P, C.c_int, C.c_int, C.c_int, C.c_int,
+                              C.c_int, _P, C.c_int, C.c_int, _P, C.c_int64, C.c_double, C.c_int,
+                              C.c_int, _P, _P, _P, C.c_int]),
     "oracle_epilogue_f32": (None, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _P]),
     "oracle_epilogue_f64": (None, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _P]),
     "oracle_max_threads": (C.c_int, []),
@@ -92,6 +101,15 @@ def _p(a):
 def geometry(g: dict) -> Geometry:
     return Geometry(g["L"], g["thetac"], g["delta"], g["numsx"], g["numsy"], g["xpc"], g["ypc"],
                     g["sig"])
+
+
+def geometry_d(g: dict) -> GeometryD:
+    """Binary64 geometry.  The float fields of the reference's namelist are
+    taken at their float values unless the dict holds exact=True (finite
+    differences step the geometry in binary64)."""
+    f = (lambda v: float(v)) if g.get("exact") else (lambda v: float(np.float32(v)))
+    return GeometryD(f(g["L"]), f(g["thetac"]), f(g["delta"]), g["numsx"], g["numsy"],
+                     f(g["xpc"]), f(g["ypc"]), float(np.float32(g["sig"])))
 
 
 def lambert_inverse_f32(xyz):
@@ -166,8 +184,9 @@ class Detector:
         ny, nx = geom["numsy"], geom["numsx"]
         self.rg32 = [np.zeros((ny, nx), np.float32) for _ in range(3)]
         lib().oracle_detector_f32(C.byref(g), *(_p(a) for a in self.rg32))
+        self._gd = geometry_d(geom)
         self.rg64 = [np.zeros((ny, nx), np.float64) for _ in range(3)]
-        lib().oracle_detector_f64(C.byref(g), *(_p(a) for a in self.rg64))
+        lib().oracle_detector_f64(C.byref(self._gd), *(_p(a) for a in self.rg64))
         acc = np.ascontiguousarray(accum_e, np.int32)
         gy, gx, nE = acc.shape
         self.nE, self.Emin, self.Emax = nE, Emin, Emax
@@ -176,7 +195,8 @@ class Detector:
         self.num_el = lib().oracle_mc_weights_f32(C.byref(g), *(_p(a) for a in self.rg32), _p(acc),
                                                   nE, self.nsx, self.nsy, Emin, Emax, _p(self.W32))
         self.W64 = np.zeros((ny, nx, nE), np.float64)
-        self.Wsum64 = lib().oracle_mc_weights_f64(C.byref(g), *(_p(a) for a in self.rg64),
+        self.accum_e = acc
+        self.Wsum64 = lib().oracle_mc_weights_f64(C.byref(self._gd), *(_p(a) for a in self.rg64),
                                                   _p(acc), nE, self.nsx, self.nsy, Emin, Emax,
                                                   _p(self.W64))
 
@@ -208,14 +228,52 @@ class Detector:
     def patterns_f64(self, sr, quats, prefactor, nthreads=1):
         s = np.ascontiguousarray(sr, np.float32)
         nE, gy, gx = s.shape
-        q = np.ascontiguousarray(quats, np.float32)
+        q = np.ascontiguousarray(quats, np.float64)
         n = q.shape[0]
         ny, nx = self.geom["numsy"], self.geom["numsx"]
         out = np.zeros((n, ny, nx), np.float64)
-        lib().oracle_patterns_f64(C.byref(self._g), *(_p(a) for a in self.rg64), _p(self.W64),
+        lib().oracle_patterns_f64(C.byref(self._gd), *(_p(a) for a in self.rg64), _p(self.W64),
                                   self.nE, self.Emin, self.Emax, _p(s), (gx - 1) // 2,
                                   (gy - 1) // 2, _p(q), n, prefactor, _p(out), nthreads)
         return out
+
+
+def vjp_f64(geom: dict, accum_e, Emin, Emax, sr, quats, prefactor, binning, mode, data,
+            nthreads=None):
+    """Analytic FP64 gradient per pattern with respect to (w0, w1, w2, xpc,
+    ypc, L).  mode "cot": data is the cotangent on the output records; mode
+    "ndp": data are target records and the loss is 1 - normalised dot
+    product.  Returns (loss[N], grad[N, 6])."""
+    g = geometry_d(geom)
+    acc = np.ascontiguousarray(accum_e, np.int32)
+    gyy, gxx, nE = acc.shape
+    s = np.ascontiguousarray(sr, np.float32)
+    _, gy, gx = s.shape
+    q = np.ascontiguousarray(quats, np.float64)
+    n = q.shape[0]
+    d = np.ascontiguousarray(data, np.float32)
+    loss = np.zeros(n)
+    grad = np.zeros((n, 6))
+    nt = max_threads() if nthreads is None else nthreads
+    lib().oracle_vjp_f64(C.byref(g), _p(acc), nE, (gxx - 1) // 2, (gyy - 1) // 2, Emin, Emax,
+                         _p(s), (gx - 1) // 2, (gy - 1) // 2, _p(q), n, prefactor, binning,
+                         0 if mode == "cot" else 1, _p(d), _p(loss), _p(grad), nt)
+    return loss, grad
+
+
+def rotate_left(q, w):
+    """exp(w) (x) q in binary64 (scalar-first), the rotation tangent used by
+    the derivatives: exp(w) = (cos|w|/2, sin(|w|/2) w/|w|)."""
+    q = np.asarray(q, np.float64)
+    w = np.asarray(w, np.float64)
+    th = np.linalg.norm(w)
+    e = np.array([1.0, 0.0, 0.0, 0.0]) if th == 0 else \
+        np.concatenate([[np.cos(th / 2)], np.sin(th / 2) * w / th])
+    x, y = e, q
+    return np.array([x[0] * y[0] - x[1] * y[1] - x[2] * y[2] - x[3] * y[3],
+                     x[0] * y[1] + x[1] * y[0] + x[2] * y[3] - x[3] * y[2],
+                     x[0] * y[2] - x[1] * y[3] + x[2] * y[0] + x[3] * y[1],
+                     x[0] * y[3] + x[1] * y[2] - x[2] * y[1] + x[3] * y[0]])
 
 
 def epilogue_f32(pat, binning, mode, gammavalue):
