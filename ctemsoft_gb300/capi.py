@@ -79,6 +79,7 @@ _SIGS = {
     "ebsd_set_stream": (C.c_int, [_P, _P]),
     "ebsd_set_option": (C.c_int, [_P, C.c_char_p, C.c_int64]),
     "ebsd_set_master": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "ebsd_share_master": (C.c_int, [_P, _P]),
     "ebsd_set_detector": (C.c_int, [_P, C.POINTER(Geometry), _P, C.c_int32, C.c_int32,
                                     C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     "ebsd_energy_window": (C.c_int, [C.c_float, C.c_float, C.c_double, C.c_double, C.c_int32,
@@ -201,6 +202,10 @@ class Handle:
         numset, nE, gy, gx = sr.shape
         _check(lib().ebsd_set_master(self._h, _ptr(sr), (gx - 1) // 2, (gy - 1) // 2, nE, numset),
                self._h)
+
+    def share_master(self, other: "Handle"):
+        """Use other's master pattern (same device, no copy)."""
+        _check(lib().ebsd_share_master(self._h, other._h), self._h)
 
     def set_detector(self, geom: dict, accum_e: np.ndarray, Emin: int, Emax: int) -> int:
         """accum_e: array shaped (2nsy+1, 2nsx+1, numEbins) = Fortran

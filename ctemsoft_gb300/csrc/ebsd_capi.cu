@@ -7,14 +7,35 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "ebsd_host.h"
 #include "ebsd_internal.h"
 
 using namespace ebsd;
+
+// A master pattern on one device, shared by every handle that uses it
+// (ebsd_share_master): the raw Fortran-order upload and one
+// energy-interleaved layout per energy window (first bin, bin count).
+struct MasterStore {
+    int device = 0;
+    float* raw = nullptr;
+    int npx = 0, npy = 0, nE = 0, numset = 0;
+    float max_sr = 0.0f;
+    std::map<std::pair<int, int>, std::pair<float4*, size_t>> layouts;
+    ~MasterStore()
+    {
+        cudaSetDevice(device);
+        cudaFree(raw);
+        for (auto& kv : layouts) cudaFree(kv.second.first);
+        cudaGetLastError();
+    }
+};
 
 struct ebsd_handle {
     int device = 0;
@@ -23,16 +44,14 @@ struct ebsd_handle {
     cudaStream_t copy_stream = nullptr;
     std::string err;
 
-    // master: raw Fortran-order sr summed over nothing yet (all sets)
-    float* d_master_raw = nullptr;
+    // master pattern (possibly shared with other handles on this device)
+    std::shared_ptr<MasterStore> ms;
     int npx = 0, npy = 0, nE = 0, numset = 0;
     bool have_master = false;
-    float max_sr = 0.0f;
 
-    // energy-interleaved master for the current window
+    // energy-interleaved master for the detector's window (owned by ms)
     float4* d_master_il = nullptr;
     size_t il_bytes = 0;
-    int il_e0 = -1, il_nsel = 0;
 
     // detector
     bool have_detector = false;
@@ -278,8 +297,7 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
-    cudaFree(h->d_master_raw);
-    cudaFree(h->d_master_il);
+    h->ms.reset();
     cudaFree(h->d_rg);
     cudaFree(h->d_W);
     cudaFree(h->d_drg);
@@ -361,28 +379,54 @@ extern "C" int ebsd_set_master(ebsd_handle* h, const float* sr, int32_t npx, int
     if (rc) return rc;
     const size_t n = (size_t)(2 * npx + 1) * (2 * npy + 1) * nE * numset;
     cudaStreamSynchronize(h->stream);
-    cudaFree(h->d_master_raw);
-    h->d_master_raw = nullptr;
+    h->ms.reset();
     h->have_master = false;
-    h->il_e0 = -1;
-    CK(h, cudaMalloc(&h->d_master_raw, n * sizeof(float)), "cudaMalloc master");
-    CK(h, cudaMemcpy(h->d_master_raw, sr, n * sizeof(float), cudaMemcpyHostToDevice),
-       "master upload");
-    h->npx = npx;
-    h->npy = npy;
-    h->nE = nE;
-    h->numset = numset;
+    h->have_detector = false;  // window must be rebuilt
+    h->d_master_il = nullptr;
+    auto ms = std::make_shared<MasterStore>();
+    ms->device = h->device;
+    CK(h, cudaMalloc(&ms->raw, n * sizeof(float)), "cudaMalloc master");
+    CK(h, cudaMemcpy(ms->raw, sr, n * sizeof(float), cudaMemcpyHostToDevice), "master upload");
+    ms->npx = npx;
+    ms->npy = npy;
+    ms->nE = nE;
+    ms->numset = numset;
     // maxval(sr) of the set sum, printed by the program (CTEMEBSD.f90:548)
     float mx = -INFINITY;
     const size_t plane = (size_t)(2 * npx + 1) * (2 * npy + 1) * nE;
     for (size_t i = 0; i < plane; ++i) {
-        float s = 0.0f;
-        for (int st = 0; st < numset; ++st) s = s + sr[i + plane * st];
-        mx = std::max(mx, s);
+        float sum = 0.0f;
+        for (int st = 0; st < numset; ++st) sum = sum + sr[i + plane * st];
+        mx = std::max(mx, sum);
     }
-    h->max_sr = mx;
+    ms->max_sr = mx;
+    h->ms = std::move(ms);
+    h->npx = npx;
+    h->npy = npy;
+    h->nE = nE;
+    h->numset = numset;
     h->have_master = true;
-    if (h->have_detector) h->have_detector = false;  // window must be rebuilt
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_share_master(ebsd_handle* dst, const ebsd_handle* src)
+{
+    if (!dst || !src) return set_err(dst, EBSD_EINVAL, "ebsd_share_master: null handle");
+    if (!src->have_master)
+        return set_err(dst, EBSD_ESTATE, "ebsd_share_master: the source handle has no master");
+    if (src->device != dst->device)
+        return set_err(dst, EBSD_EINVAL, "ebsd_share_master: handles are on devices %d and %d",
+                       src->device, dst->device);
+    cudaSetDevice(dst->device);
+    cudaStreamSynchronize(dst->stream);
+    dst->ms = src->ms;
+    dst->npx = src->npx;
+    dst->npy = src->npy;
+    dst->nE = src->nE;
+    dst->numset = src->numset;
+    dst->have_master = true;
+    dst->have_detector = false;
+    dst->d_master_il = nullptr;
     return EBSD_OK;
 }
 
@@ -444,16 +488,24 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
     CK(h, cudaMalloc(&h->d_dW, sizeof(float4) * (size_t)P * 3 * NV), "cudaMalloc dW");
 
     // master re-layout for this window
-    if (h->il_e0 != Emin - 1 || h->il_nsel != nsel) {
-        cudaFree(h->d_master_il);
-        h->d_master_il = nullptr;
-        h->il_bytes = sizeof(float4) * (size_t)(2 * h->npx + 1) * (2 * h->npy + 1) * NV;
-        CK(h, cudaMalloc(&h->d_master_il, h->il_bytes), "cudaMalloc master layout");
-        CK(h, launch_master_relayout(h->d_master_raw, h->npx, h->npy, h->nE, h->numset, Emin - 1,
-                                     nsel, NV, h->d_master_il, s),
-           "master re-layout");
-        h->il_e0 = Emin - 1;
-        h->il_nsel = nsel;
+    {
+        const auto key = std::make_pair(Emin - 1, nsel);
+        auto it = h->ms->layouts.find(key);
+        if (it == h->ms->layouts.end()) {
+            const size_t bytes =
+                sizeof(float4) * (size_t)(2 * h->npx + 1) * (2 * h->npy + 1) * NV;
+            float4* il = nullptr;
+            CK(h, cudaMalloc(&il, bytes), "cudaMalloc master layout");
+            cudaError_t e2 = launch_master_relayout(h->ms->raw, h->npx, h->npy, h->nE, h->numset,
+                                                    Emin - 1, nsel, NV, il, s);
+            if (e2 != cudaSuccess) {
+                cudaFree(il);
+                return cuda_err(h, e2, "master re-layout");
+            }
+            it = h->ms->layouts.emplace(key, std::make_pair(il, bytes)).first;
+        }
+        h->d_master_il = it->second.first;
+        h->il_bytes = it->second.second;
     }
 
     float ca, sa;
@@ -823,7 +875,7 @@ extern "C" int ebsd_get_detector(ebsd_handle* h, float* W, float* rgx, float* rg
 // Internal accessors for the program driver (ebsd_program.cpp).
 namespace ebsd {
 namespace host {
-float handle_max_sr(const ebsd_handle* h) { return h->max_sr; }
+float handle_max_sr(const ebsd_handle* h) { return h->ms ? h->ms->max_sr : 0.0f; }
 int handle_set_error(ebsd_handle* h, int code, const char* msg)
 {
     return set_err(h, code, "%s", msg);

@@ -223,30 +223,53 @@ cudaError_t launch_weights(const float4* rg, int P, const int32_t* accum_e, int 
 
 // num_el = nint(sum(accum_e_detector)), CTEMEBSD.f90:516.  gfortran sums
 // the array sequentially in single precision in memory order (bin fastest,
-// then x, then y); bins outside the window add exact zeros.  One thread
-// reproduces that order; it runs once per detector.
+// then x, then y); bins outside the window add exact zeros.  That order is
+// one dependent chain of adds, so one lane performs it; the warp stages the
+// next chunk of 32 pixels through shared memory (double-buffered) so the
+// chain never waits on global memory.  Runs once per detector.
+constexpr int kNumElChunk = 32;
+
 __global__ void k_num_el(const float4* __restrict__ W, int P, int nsel, int NV,
                          float* __restrict__ out)
 {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    extern __shared__ float4 stage[];  // [2][NV][32]
+    const int lane = threadIdx.x;
+    const int nchunks = (P + kNumElChunk - 1) / kNumElChunk;
+    auto load = [&](int ch, int buf) {
+        const int p = ch * kNumElChunk + lane;
+        for (int c = 0; c < NV; ++c)
+            stage[(buf * NV + c) * kNumElChunk + lane] =
+                p < P ? W[(int64_t)c * P + p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    };
     float s = 0.0f;
-    for (int p = 0; p < P; ++p) {
-        for (int c = 0; c < NV; ++c) {
-            const float4 w = W[(int64_t)c * P + p];
-            const int k = 4 * c;
-            if (k + 0 < nsel) s = s + w.x;
-            if (k + 1 < nsel) s = s + w.y;
-            if (k + 2 < nsel) s = s + w.z;
-            if (k + 3 < nsel) s = s + w.w;
+    if (nchunks > 0) load(0, 0);
+    __syncwarp();
+    for (int ch = 0; ch < nchunks; ++ch) {
+        const int buf = ch & 1;
+        if (ch + 1 < nchunks) load(ch + 1, buf ^ 1);
+        if (lane == 0) {
+            const int np = min(kNumElChunk, P - ch * kNumElChunk);
+            for (int j = 0; j < np; ++j) {
+                for (int c = 0; c < NV; ++c) {
+                    const float4 w = stage[(buf * NV + c) * kNumElChunk + j];
+                    const int k = 4 * c;
+                    if (k + 0 < nsel) s = s + w.x;
+                    if (k + 1 < nsel) s = s + w.y;
+                    if (k + 2 < nsel) s = s + w.z;
+                    if (k + 3 < nsel) s = s + w.w;
+                }
+            }
         }
+        __syncwarp();
     }
-    *out = s;
+    if (lane == 0) *out = s;
 }
 
 cudaError_t launch_num_el(const float4* W, int P, int nsel, int NV, float* sum_out,
                           cudaStream_t s)
 {
-    k_num_el<<<1, 32, 0, s>>>(W, P, nsel, NV, sum_out);
+    const size_t smem = sizeof(float4) * 2 * NV * kNumElChunk;
+    k_num_el<<<1, 32, smem, s>>>(W, P, nsel, NV, sum_out);
     return cudaGetLastError();
 }
 

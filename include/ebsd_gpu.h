@@ -104,6 +104,12 @@ int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value);
 int ebsd_set_master(ebsd_handle* h, const float* sr, int32_t npx, int32_t npy, int32_t nE,
                     int32_t numset);
 
+/* Let handle dst use the master pattern of src (same device) without a
+ * copy: several detectors (each its own handle) share one device master
+ * and its energy-interleaved layouts.  No reference counterpart (the
+ * reference runs one detector per process). */
+int ebsd_share_master(ebsd_handle* dst, const ebsd_handle* src);
+
 /* Detector set-up: the scintillator direction cosines (CTEMEBSD.f90:416-452)
  * and the Monte-Carlo energy weights accum_e_detector (:476-510) for bins
  * Emin..Emax (1-based, inclusive, from ebsd_energy_window).  accum_e is the
