@@ -90,6 +90,8 @@ _SIGS = {
     "ebsd_forward": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P]),
     "ebsd_cells": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P, _P]),
     "ebsd_vjp": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), C.c_int32, _P, _P, _P]),
+    "ebsd_vjp_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), C.c_int32, _P, _P,
+                                   _P]),
     "ebsd_get_detector": (C.c_int, [_P, _P, _P, _P, _P]),
     "ebsd_run_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "ebsd_read_mc_file": (C.c_int, [C.c_char_p, C.POINTER(MCHeader), _P]),

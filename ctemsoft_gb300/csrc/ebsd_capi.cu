@@ -9,6 +9,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <utility>
@@ -779,6 +780,120 @@ extern "C" int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebs
             CK(h, cudaMemcpyAsync(loss + o0, dloss, sizeof(float) * m, cudaMemcpyDeviceToHost, s),
                "loss copy");
         if (!qdev || !ddev || !gdev || !ldev) CK(h, cudaStreamSynchronize(s), "adjoint");
+    }
+    return EBSD_OK;
+}
+
+// ----------------------------------------------------------------------
+// Adjoint without allocation.
+//
+// Some callers cannot let this library allocate device memory while they
+// run the adjoint: a host that owns all GPU memory through its own pool
+// (an indexing or refinement framework whose caching allocator must stay
+// the only allocator on the device), and a refinement loop that cannot
+// afford the device-wide synchronisation cudaMalloc/cudaFree may cause in
+// the middle of its iterations.  ebsd_vjp_noalloc serves them: the caller
+// passes device buffers for every input and output, and the per-CTA
+// partial sums go to the fixed array below instead of a handle-owned
+// buffer.  The handle's master and detector tables were allocated earlier,
+// by ebsd_set_master / ebsd_set_detector, not by this call.
+
+// 8 MiB of partial sums, resident on every GPU that loads the library until
+// the process exits.  One orientation needs ntiles * K floats (ntiles =
+// ceil(numsx/32) * ceil(numsy/8), K = 15 in loss mode, 6 in cotangent mode),
+// so a 640x480 detector fits 116 orientations per launch; larger batches
+// run as several launches through the same array.
+constexpr size_t kNoAllocScratchFloats = size_t(2) << 20;
+static __device__ __align__(256) float g_vjp_scratch[kNoAllocScratchFloats];
+
+namespace {
+constexpr int kMaxDevicesNoAlloc = 64;
+std::mutex g_scratch_mu;
+float* g_scratch_addr[kMaxDevicesNoAlloc] = {};
+
+// Device address of g_vjp_scratch on the current device (host code may
+// only use the symbol through this address).  Looked up once per device.
+int scratch_address(ebsd_handle* h, float** out)
+{
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (h->device < 0 || h->device >= kMaxDevicesNoAlloc)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_vjp_noalloc: device %d beyond %d", h->device,
+                       kMaxDevicesNoAlloc);
+    if (!g_scratch_addr[h->device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_vjp_scratch);
+        if (e != cudaSuccess || !ptr) {
+            cudaGetLastError();
+            return set_err(h, EBSD_ECUDA, "ebsd_vjp_noalloc: scratch address lookup failed: %s",
+                           cudaGetErrorString(e));
+        }
+        g_scratch_addr[h->device] = (float*)ptr;
+    }
+    *out = g_scratch_addr[h->device];
+    return EBSD_OK;
+}
+}  // namespace
+
+extern "C" int ebsd_vjp_noalloc(ebsd_handle* h, const float* quats, int64_t n,
+                                const ebsd_epilogue* e, int32_t mode, const float* data,
+                                float* loss, float* grad)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n < 0) return set_err(h, EBSD_EINVAL, "negative orientation count");
+    if (n == 0) return EBSD_OK;
+    if (!quats || !e || !data || !grad)
+        return set_err(h, EBSD_EINVAL, "ebsd_vjp_noalloc: null argument");
+    if (mode != EBSD_VJP_COTANGENT && mode != EBSD_VJP_NDP)
+        return set_err(h, EBSD_EINVAL, "ebsd_vjp_noalloc: unknown mode %d", mode);
+    if (e->scalingmode == EBSD_SCALING_GAM || e->poisson)
+        return set_err(h, EBSD_EUNSUPPORTED,
+                       "ebsd_vjp_noalloc: gamma and noise epilogues have no adjoint");
+    if (h->NV > 8)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_vjp_noalloc: at most 32 energy bins");
+    if (ptr_kind(quats) != kDevice || ptr_kind(data) != kDevice || ptr_kind(grad) != kDevice ||
+        (loss && ptr_kind(loss) != kDevice))
+        return set_err(h, EBSD_EINVAL,
+                       "ebsd_vjp_noalloc: quats, data, loss and grad must be device memory");
+    rc = activate(h);
+    if (rc) return rc;
+    float* scratch = nullptr;
+    rc = scratch_address(h, &scratch);
+    if (rc) return rc;
+    FwdParams p;
+    rc = fill_params(h, e, p);
+    if (rc) return rc;
+    VjpParams vp;
+    memset(&vp, 0, sizeof vp);
+    vp.drg = h->d_drg;
+    vp.dW = h->d_dW;
+    vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
+    vp.opc = 2;
+    const int tile_y = 8;
+    if (vp.binning > tile_y)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_vjp_noalloc: binning %d exceeds the tile",
+                       vp.binning);
+    const int K = mode == EBSD_VJP_NDP ? 15 : 6;
+    const size_t per_o = (size_t)vjp_tiles(p, tile_y) * K;
+    if (per_o > kNoAllocScratchFloats)
+        return set_err(h, EBSD_EUNSUPPORTED,
+                       "ebsd_vjp_noalloc: one orientation of this %dx%d detector needs %zu "
+                       "floats of scratch, more than the fixed %zu",
+                       p.numsx, p.numsy, per_o, kNoAllocScratchFloats);
+    // every partial a launch reads is written by the same launch first, so
+    // the array needs no clearing between calls
+    const int64_t chunk = (int64_t)(kNoAllocScratchFloats / per_o);
+    const size_t rec = (size_t)p.out_nx * p.out_ny;
+    for (int64_t o0 = 0; o0 < n; o0 += chunk) {
+        const int64_t m = std::min<int64_t>(chunk, n - o0);
+        p.n = m;
+        p.quats = (const float4*)quats + o0;
+        vp.data = data + (size_t)o0 * rec;
+        vp.partial = scratch;
+        vp.grad = grad + 6 * o0;
+        vp.loss = loss ? loss + o0 : nullptr;
+        cudaError_t ce = launch_vjp(p, vp, h->NV, mode, tile_y, h->stream);
+        if (ce != cudaSuccess) return cuda_err(h, ce, "ebsd_vjp_noalloc launch");
     }
     return EBSD_OK;
 }

@@ -160,6 +160,26 @@ int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilo
 int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e, int32_t mode,
              const float* data, float* loss, float* grad);
 
+/* ebsd_vjp for callers that cannot let the library allocate device memory
+ * during the call -- hosts whose GPU memory is owned by their own pool or
+ * caching allocator, and refinement loops that cannot afford the device
+ * synchronisation cudaMalloc/cudaFree may cause.  It has no counterpart in
+ * the reference.  Same arguments and results as ebsd_vjp, but quats, data,
+ * loss (if not NULL) and grad must be device memory, and the call itself
+ * allocates nothing: its per-CTA partial sums live in one fixed 8 MiB
+ * device array that every GPU loading the library holds until the process
+ * exits.  A detector needing more than that for a single orientation
+ * (ceil(numsx/32)*ceil(numsy/8)*15 floats in EBSD_VJP_NDP mode, *6 in
+ * cotangent mode) is rejected with EBSD_EUNSUPPORTED; larger batches run as
+ * several launches through the array.  The first call on a device looks up
+ * the array's device address (a one-time set-up), so make that first call
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU (other streams, other threads, other handles) race
+ * and must be serialised by the caller.  Work is queued on the handle's
+ * stream and the call returns without waiting for it. */
+int ebsd_vjp_noalloc(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
+                     int32_t mode, const float* data, float* loss, float* grad);
+
 /* Lambert cells of the loop (CTEMEBSD.f90:584-598) for n quaternions:
  * nix/niy (grid indices in -npx..npx) and the scaled Lambert coordinates
  * ixy0/ixy1, each [n][numsy][numsx].  Host or device pointers.  For parity
