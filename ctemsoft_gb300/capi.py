@@ -45,6 +45,14 @@ class Epilogue(C.Structure):
                 ("gammavalue", C.c_float), ("poisson", C.c_int32), ("seed", C.c_uint64)]
 
 
+class Job(C.Structure):
+    _fields_ = [("source", C.c_void_p), ("quats", C.c_void_p), ("n", C.c_int64),
+                ("epilogue", Epilogue), ("out", C.c_void_p)]
+
+
+BATCH_GRAPH = 1
+
+
 class MCHeader(C.Structure):
     _fields_ = [("numEbins", C.c_int32), ("numzbins", C.c_int32), ("numsx", C.c_int32),
                 ("numsy", C.c_int32), ("num_el_total", C.c_int64), ("nthreads", C.c_int32),
@@ -89,6 +97,10 @@ _SIGS = {
                                    C.POINTER(C.c_int32)]),
     "ebsd_forward": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P]),
     "ebsd_cells": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P, _P]),
+    "ebsd_forward_batched": (C.c_int, [_P, C.POINTER(Job), C.c_int32, C.c_int32]),
+    "ebsd_autotune": (C.c_int, [_P, C.POINTER(Epilogue), C.c_int64, C.c_char_p,
+                                C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                C.POINTER(C.c_float)]),
     "ebsd_vjp": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), C.c_int32, _P, _P, _P]),
     "ebsd_vjp_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), C.c_int32, _P, _P,
                                    _P]),
@@ -259,6 +271,25 @@ class Handle:
         _check(lib().ebsd_vjp(self._h, _ptr(quats), n, C.byref(epi), m, _ptr(data), _ptr(loss),
                               _ptr(grad)), self._h)
         return loss, grad
+
+    def autotune(self, epi: Epilogue, n_sample: int = 64, cache_path=None):
+        """Pick (and apply) the fastest launch shape; returns (tile_y,
+        orient_per_cta, us_per_pattern)."""
+        ty, oc, us = C.c_int32(), C.c_int32(), C.c_float()
+        _check(lib().ebsd_autotune(self._h, C.byref(epi), n_sample,
+                                   None if cache_path is None else str(cache_path).encode(),
+                                   C.byref(ty), C.byref(oc), C.byref(us)), self._h)
+        return ty.value, oc.value, us.value
+
+    def forward_batched(self, jobs, graph: bool = False):
+        """jobs: list of (source Handle, device quats tensor, Epilogue, device
+        out tensor).  Queued on this handle's stream."""
+        arr = (Job * max(1, len(jobs)))()
+        for i, (src, q, epi, out) in enumerate(jobs):
+            arr[i] = Job(src.raw.value if hasattr(src.raw, "value") else src.raw, _ptr(q),
+                         int(q.shape[0]), epi, _ptr(out))
+        _check(lib().ebsd_forward_batched(self._h, arr, len(jobs), BATCH_GRAPH if graph else 0),
+               self._h)
 
     def cells(self, quats: np.ndarray):
         q = np.ascontiguousarray(quats, dtype=np.float32)

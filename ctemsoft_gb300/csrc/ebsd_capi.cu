@@ -83,6 +83,15 @@ struct ebsd_handle {
     LaunchCfg cfg;
     int weights_fp64 = 1;
     int lambert_accurate = 0;
+
+    // batched pattern loop: device job table, pinned host mirror, graph
+    DeviceBuf batch_table;
+    void* batch_table_host = nullptr;
+    size_t batch_table_host_bytes = 0;
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<int> batch_key;
+    cudaStream_t batch_stream = nullptr;
+    std::map<int, int> batch_grid;  // NV -> persistent grid size
 };
 
 namespace {
@@ -313,6 +322,9 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
         if (h->ev_d2h[i]) cudaEventDestroy(h->ev_d2h[i]);
     }
     cudaFree(h->tmp.ptr);
+    cudaFree(h->batch_table.ptr);
+    if (h->batch_table_host) cudaFreeHost(h->batch_table_host);
+    if (h->batch_exec) cudaGraphExecDestroy(h->batch_exec);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     cudaGetLastError();
@@ -895,6 +907,305 @@ extern "C" int ebsd_vjp_noalloc(ebsd_handle* h, const float* quats, int64_t n,
         cudaError_t ce = launch_vjp(p, vp, h->NV, mode, tile_y, h->stream);
         if (ce != cudaSuccess) return cuda_err(h, ce, "ebsd_vjp_noalloc launch");
     }
+    return EBSD_OK;
+}
+
+// ----------------------------------------------------------------------
+// Batched pattern loop
+
+namespace {
+
+struct BatchGroup {
+    int NV;
+    std::vector<BatchJob> jobs;
+};
+
+}  // namespace
+
+extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_t njobs,
+                                    int32_t flags)
+{
+    if (!h) return set_err(nullptr, EBSD_EINVAL, "null handle");
+    if (njobs < 0 || (njobs > 0 && !jobs))
+        return set_err(h, EBSD_EINVAL, "ebsd_forward_batched: bad job list");
+    int rc = activate(h);
+    if (rc) return rc;
+    std::vector<BatchGroup> groups;
+    for (int j = 0; j < njobs; ++j) {
+        const ebsd_job& J = jobs[j];
+        ebsd_handle* src = J.source;
+        if (!src || !src->have_master || !src->have_detector)
+            return set_err(h, EBSD_ESTATE, "job %d: source handle has no master/detector", j);
+        if (src->device != h->device)
+            return set_err(h, EBSD_EINVAL, "job %d is on device %d, the batch runs on %d", j,
+                           src->device, h->device);
+        if (J.n < 0) return set_err(h, EBSD_EINVAL, "job %d: negative orientation count", j);
+        if (J.n == 0) continue;
+        if (!J.quats || !J.out) return set_err(h, EBSD_EINVAL, "job %d: null pointer", j);
+        if (ptr_kind(J.quats) != kDevice || ptr_kind(J.out) != kDevice)
+            return set_err(h, EBSD_EINVAL, "job %d: quats and out must be device memory", j);
+        if (src->NV > 8)
+            return set_err(h, EBSD_EUNSUPPORTED, "job %d: more than 32 energy bins", j);
+        BatchJob b;
+        memset(&b, 0, sizeof b);
+        rc = fill_params(src, &J.epilogue, b.p);
+        if (rc) return set_err(h, rc, "job %d: %s", j, src->err.c_str());
+        b.p.quats = (const float4*)J.quats;
+        b.p.out = J.out;
+        b.p.n = J.n;
+        b.tiles_x = (b.p.numsx + kTileX - 1) / kTileX;
+        b.ntiles = b.tiles_x * ((b.p.numsy + kBatchTileY - 1) / kBatchTileY);
+        b.opc = std::max(1, src->cfg.orient_per_cta);
+        b.items = (long long)b.ntiles * ((J.n + b.opc - 1) / b.opc);
+        auto g = std::find_if(groups.begin(), groups.end(),
+                              [&](const BatchGroup& x) { return x.NV == src->NV; });
+        if (g == groups.end()) {
+            groups.push_back({src->NV, {}});
+            g = groups.end() - 1;
+        }
+        g->jobs.push_back(b);
+    }
+    if (groups.empty()) return EBSD_OK;
+    std::sort(groups.begin(), groups.end(),
+              [](const BatchGroup& a, const BatchGroup& b) { return a.NV < b.NV; });
+
+    // table: [headers][counters][jobs of group 0][jobs of group 1]...
+    const size_t G = groups.size();
+    size_t njob_total = 0;
+    for (auto& g : groups) njob_total += g.jobs.size();
+    const size_t hdr_bytes = G * sizeof(BatchHeader);
+    const size_t cnt_off = (hdr_bytes + 255) & ~size_t(255);
+    const size_t job_off = (cnt_off + G * sizeof(unsigned long long) + 255) & ~size_t(255);
+    const size_t bytes = job_off + njob_total * sizeof(BatchJob);
+
+    // the previous batch must have consumed the pinned table before it is rewritten
+    CK(h, cudaStreamSynchronize(h->stream), "batch");
+    std::vector<int> key;
+    for (auto& g : groups) {
+        key.push_back(g.NV);
+        key.push_back((int)g.jobs.size());
+    }
+    const bool use_graph = (flags & EBSD_BATCH_GRAPH) != 0;
+    const bool reuse = use_graph && h->batch_exec && h->batch_key == key &&
+                       h->batch_table_host_bytes >= bytes && h->batch_stream == h->stream;
+    if (!reuse) {
+        if (h->batch_exec) {
+            cudaGraphExecDestroy(h->batch_exec);
+            h->batch_exec = nullptr;
+        }
+        rc = ensure(h, h->batch_table, bytes, "batch table");
+        if (rc) return rc;
+        if (h->batch_table_host_bytes < bytes) {
+            if (h->batch_table_host) cudaFreeHost(h->batch_table_host);
+            h->batch_table_host = nullptr;
+            h->batch_table_host_bytes = 0;
+            CK(h, cudaMallocHost(&h->batch_table_host, bytes), "pinned batch table");
+            h->batch_table_host_bytes = bytes;
+        }
+    }
+    // fill the pinned table
+    char* ht = (char*)h->batch_table_host;
+    char* dt = (char*)h->batch_table.ptr;
+    memset(ht, 0, bytes);
+    size_t jo = 0;
+    std::vector<int> grids(G);
+    for (size_t gi = 0; gi < G; ++gi) {
+        auto& g = groups[gi];
+        long long begin = 0;
+        for (auto& b : g.jobs) {
+            b.item_begin = begin;
+            begin += b.items;
+        }
+        BatchHeader hd;
+        memset(&hd, 0, sizeof hd);
+        hd.total_items = begin;
+        hd.njobs = (int)g.jobs.size();
+        memcpy(ht + gi * sizeof(BatchHeader), &hd, sizeof hd);
+        memcpy(ht + job_off + jo * sizeof(BatchJob), g.jobs.data(), g.jobs.size() * sizeof(BatchJob));
+        jo += g.jobs.size();
+        auto it = h->batch_grid.find(g.NV);
+        if (it == h->batch_grid.end()) it = h->batch_grid.emplace(g.NV, batched_grid(g.NV)).first;
+        grids[gi] = it->second;
+    }
+    cudaStream_t s = h->stream;
+    auto enqueue = [&]() -> cudaError_t {
+        cudaError_t e = cudaMemcpyAsync(dt, ht, bytes, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(dt + cnt_off, 0, G * sizeof(unsigned long long), s);
+        size_t j0 = 0;
+        for (size_t gi = 0; gi < G && e == cudaSuccess; ++gi) {
+            e = launch_forward_batched(
+                (const BatchJob*)(dt + job_off + j0 * sizeof(BatchJob)),
+                (const BatchHeader*)(dt + gi * sizeof(BatchHeader)),
+                (unsigned long long*)(dt + cnt_off) + gi, groups[gi].NV, grids[gi], s);
+            j0 += groups[gi].jobs.size();
+        }
+        return e;
+    };
+    if (!use_graph) {
+        cudaError_t e = enqueue();
+        if (e != cudaSuccess) return cuda_err(h, e, "batched launch");
+        return EBSD_OK;
+    }
+    if (!reuse) {
+        cudaGraph_t graph = nullptr;
+        CK(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "graph capture");
+        cudaError_t e = enqueue();
+        cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return cuda_err(h, e != cudaSuccess ? e : e2, "graph capture");
+        }
+        e = cudaGraphInstantiate(&h->batch_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            h->batch_exec = nullptr;
+            return cuda_err(h, e, "graph instantiate");
+        }
+        h->batch_key = key;
+        h->batch_stream = s;
+    }
+    CK(h, cudaGraphLaunch(h->batch_exec, s), "graph launch");
+    return EBSD_OK;
+}
+
+// ----------------------------------------------------------------------
+// Launch-shape autotuner
+
+namespace {
+
+std::string tune_key(ebsd_handle* h, const FwdParams& p)
+{
+    int sms = 0, major = 0, minor = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, h->device);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, h->device);
+    char buf[256];
+    snprintf(buf, sizeof buf, "sm%d%d_x%d det%dx%d nv%d bin%d mode%d strict%d acc%d", major, minor,
+             sms, p.numsx, p.numsy, h->NV, p.binning, p.mode, (int)h->cfg.strict, p.accurate);
+    return buf;
+}
+
+bool tune_lookup(const char* path, const std::string& key, int* ty, int* opc, float* us)
+{
+    if (!path) return false;
+    FILE* f = fopen(path, "r");
+    if (!f) return false;
+    char line[512];
+    bool found = false;
+    while (fgets(line, sizeof line, f)) {
+        char* bar = strchr(line, '|');
+        if (!bar) continue;
+        *bar = 0;
+        if (key != line) continue;
+        int a, b;
+        float c;
+        if (sscanf(bar + 1, "%d|%d|%f", &a, &b, &c) == 3) {
+            *ty = a;
+            *opc = b;
+            *us = c;
+            found = true;  // the last entry for a key wins
+        }
+    }
+    fclose(f);
+    return found;
+}
+
+}  // namespace
+
+extern "C" int ebsd_autotune(ebsd_handle* h, const ebsd_epilogue* e, int64_t n_sample,
+                             const char* cache_path, int32_t* tile_y, int32_t* opc,
+                             float* us_per_pattern)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!e || n_sample < 1) return set_err(h, EBSD_EINVAL, "ebsd_autotune: invalid arguments");
+    rc = activate(h);
+    if (rc) return rc;
+    FwdParams p;
+    rc = fill_params(h, e, p);
+    if (rc) return rc;
+    const std::string key = tune_key(h, p);
+    int best_ty = 0, best_opc = 0;
+    float best_us = 0.0f;
+    if (!tune_lookup(cache_path, key, &best_ty, &best_opc, &best_us)) {
+        // sample orientations: a fixed pseudo-random set of unit quaternions
+        std::vector<float> q(4 * (size_t)n_sample);
+        uint64_t st = 0x9E3779B97F4A7C15ull;
+        auto rnd = [&]() {
+            st ^= st << 13;
+            st ^= st >> 7;
+            st ^= st << 17;
+            return (double)(st >> 11) * (1.0 / 9007199254740992.0);
+        };
+        for (int64_t i = 0; i < n_sample; ++i) {
+            const double u1 = rnd(), u2 = rnd(), u3 = rnd();
+            const double a = std::sqrt(1.0 - u1), b = std::sqrt(u1);
+            q[4 * i + 0] = (float)(b * std::cos(2 * M_PI * u3));
+            q[4 * i + 1] = (float)(a * std::sin(2 * M_PI * u2));
+            q[4 * i + 2] = (float)(a * std::cos(2 * M_PI * u2));
+            q[4 * i + 3] = (float)(b * std::sin(2 * M_PI * u3));
+        }
+        const size_t rec = (size_t)p.out_nx * p.out_ny;
+        float4* dq = nullptr;
+        float* dout = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cudaError_t ce = cudaMalloc(&dq, sizeof(float4) * n_sample);
+        if (ce == cudaSuccess) ce = cudaMalloc(&dout, sizeof(float) * rec * n_sample);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpy(dq, q.data(), sizeof(float4) * n_sample, cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+        if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+        const LaunchCfg saved = h->cfg;
+        p.quats = dq;
+        p.out = dout;
+        p.n = n_sample;
+        best_us = INFINITY;
+        const int tys[3] = {4, 8, 16};
+        const int opcs[4] = {1, 2, 4, 8};
+        for (int ty : tys) {
+            if (ce != cudaSuccess) break;
+            if (p.binning > 1 && p.mode != EBSD_SCALING_NOT && ty % p.binning != 0) continue;
+            for (int oc : opcs) {
+                h->cfg.tile_y = ty;
+                h->cfg.orient_per_cta = oc;
+                ce = launch_forward(p, h->NV, h->cfg, h->stream);  // warm-up
+                if (ce != cudaSuccess) break;
+                ce = cudaEventRecord(e0, h->stream);
+                for (int r = 0; r < 3 && ce == cudaSuccess; ++r)
+                    ce = launch_forward(p, h->NV, h->cfg, h->stream);
+                if (ce == cudaSuccess) ce = cudaEventRecord(e1, h->stream);
+                if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+                if (ce != cudaSuccess) break;
+                const float us = 1000.0f * ms / (3.0f * (float)n_sample);
+                if (us < best_us) {
+                    best_us = us;
+                    best_ty = ty;
+                    best_opc = oc;
+                }
+            }
+        }
+        h->cfg = saved;
+        cudaFree(dq);
+        cudaFree(dout);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (ce != cudaSuccess) return cuda_err(h, ce, "ebsd_autotune");
+        if (cache_path) {
+            FILE* f = fopen(cache_path, "a");
+            if (f) {
+                fprintf(f, "%s|%d|%d|%.4f\n", key.c_str(), best_ty, best_opc, best_us);
+                fclose(f);
+            }
+        }
+    }
+    h->cfg.tile_y = best_ty;
+    h->cfg.orient_per_cta = best_opc;
+    if (tile_y) *tile_y = best_ty;
+    if (opc) *opc = best_opc;
+    if (us_per_pattern) *us_per_pattern = best_us;
     return EBSD_OK;
 }
 

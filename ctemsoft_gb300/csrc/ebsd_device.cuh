@@ -78,6 +78,55 @@ __device__ __forceinline__ void lambert_inverse(float x, float y, float z, float
     }
 }
 
+// lambert_inverse plus its Jacobian with respect to (x, y, z), sharing the
+// square root and arc tangent.  The point (X, Y) is computed by exactly the
+// operations of lambert_inverse, so cells agree with the forward kernels.
+// The Jacobian uses rho^2 = 2(x^2+y^2)/(1+z) (no cancellation at the poles)
+// and is zero where the map is intercepted (|z| = 1, non-unit input).
+__device__ __forceinline__ void lambert_inverse_jac(float x, float y, float z, float spi2,
+                                                    bool accurate, float& X, float& Y,
+                                                    float dX[3], float dY[3])
+{
+    float s = x * x;
+    s = s + y * y;
+    const float rxy = s;
+    s = s + z * z;
+    dX[0] = dX[1] = dX[2] = 0.0f;
+    dY[0] = dY[1] = dY[2] = 0.0f;
+    if (fabsf(1.0f - s) > 1.0e-6f || fabsf(z) == 1.0f) {
+        X = 0.0f;
+        Y = 0.0f;
+        return;
+    }
+    const float omz = accurate ? rxy / (1.0f + z) : 1.0f - z;
+    const bool xb = fabsf(y) <= fabsf(x);
+    const float u = xb ? x : y, v = xb ? y : x;       // |v| <= |u|
+    const float q = copysignf(sqrtf(2.0f * omz), u);
+    const float a = atanf(v / u);
+    const float along = q * spi2, across = q * a / spi2;
+    X = xb ? along : across;
+    Y = xb ? across : along;
+    if (!(rxy > 0.0f)) return;
+    const float rho = sqrtf(2.0f * rxy / (1.0f + z));
+    const float sg = copysignf(1.0f, u);
+    const float irho = 1.0f / rho;
+    const float f = sg * rho / (spi2 * rxy);
+    // d(along)/dz, d(across)/d(u, v, z)
+    const float dal_z = -sg * spi2 * irho;
+    const float dac_u = -f * v, dac_v = f * u, dac_z = -sg * a * irho / spi2;
+    if (xb) {  // along = X (u = x), across = Y (v = y)
+        dX[2] = dal_z;
+        dY[0] = dac_u;
+        dY[1] = dac_v;
+        dY[2] = dac_z;
+    } else {   // along = Y (u = y), across = X (v = x)
+        dY[2] = dal_z;
+        dX[1] = dac_u;
+        dX[0] = dac_v;
+        dX[2] = dac_z;
+    }
+}
+
 // Cell index and bilinear fractions, CTEMEBSD.f90:593-598:
 // nix = int(npx + ixy) - npx (float add, then truncation), dx = ixy - nix.
 // Returns the 0-based grid column of the lower corner, clamped to the grid.

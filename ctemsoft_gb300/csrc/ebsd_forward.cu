@@ -80,15 +80,14 @@ __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, fl
     ixy1 = scl * Y;
 }
 
+// One work item: the 32 x tile_y pixels of tile t for orientations
+// [o_begin, o_begin + opc).  `tile` is shared scratch of tile_y x 33 floats.
 template <int NV, bool STRICT>
-__global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y, int tiles_x,
-                                                 int ntiles, int opc)
+__device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, int tiles_x, int t,
+                                             int64_t o_begin, int opc, float* tile)
 {
-    extern __shared__ float tile[];  // [tile_y][33], binning only
     const int tid = threadIdx.x;
     const int tx = tid & 31, ty = tid >> 5;
-    const int t = (int)(blockIdx.x % (unsigned)ntiles);
-    const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
     const int x = (t % tiles_x) * kTileX + tx;
     const int y = (t / tiles_x) * tile_y + ty;
     const bool inside = x < prm.numsx && y < prm.numsy;
@@ -147,6 +146,59 @@ __global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y
     }
 }
 
+template <int NV, bool STRICT>
+__global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y, int tiles_x,
+                                                 int ntiles, int opc)
+{
+    extern __shared__ float tile[];  // [tile_y][33], binning only
+    const int t = (int)(blockIdx.x % (unsigned)ntiles);
+    const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
+    forward_tile<NV, STRICT>(prm, tile_y, tiles_x, t, o_begin, opc, tile);
+}
+
+// Batched pattern loop: one persistent grid works through a queue of work
+// items (job, tile, run of orientations) spanning jobs of different
+// detectors, binnings and masters.  Each CTA takes the next item with one
+// atomic increment and stops when the queue is exhausted -- no CTA waits
+// on another, so nothing can spin.  Jobs are ordered by item_begin.
+template <int NV>
+__global__ void __launch_bounds__(256) k_forward_batched(const BatchJob* __restrict__ jobs,
+                                                         const BatchHeader* __restrict__ hdr,
+                                                         unsigned long long* __restrict__ counter)
+{
+    __shared__ float tile[kBatchTileY * 33];
+    __shared__ long long s_item;
+    __shared__ int s_job;
+    const int njobs = hdr->njobs;
+    const long long total = hdr->total_items;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const long long it = (long long)atomicAdd(counter, 1ULL);
+            s_item = it;
+            if (it < total) {
+                int lo = 0, hi = njobs - 1;  // last job with item_begin <= it
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (jobs[mid].item_begin <= it)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                s_job = lo;
+            }
+        }
+        __syncthreads();
+        const long long it = s_item;
+        if (it >= total) break;
+        const BatchJob& J = jobs[s_job];
+        const long long local = it - J.item_begin;
+        const int t = (int)(local % J.ntiles);
+        const int64_t o_begin = (int64_t)(local / J.ntiles) * J.opc;
+        forward_tile<NV, false>(J.p, kBatchTileY, J.tiles_x, t, o_begin, J.opc, tile);
+        __syncthreads();
+    }
+}
+
 // Cell diagnostics: nix/niy/ixy per pixel and orientation.
 __global__ void k_cells(const FwdParams prm)
 {
@@ -194,7 +246,57 @@ cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
     return cfg.strict ? launch_nv2<NV, true>(p, cfg, s) : launch_nv2<NV, false>(p, cfg, s);
 }
 
+template <int NV>
+cudaError_t launch_batched_nv(const BatchJob* jobs, const BatchHeader* hdr,
+                              unsigned long long* counter, int grid, cudaStream_t s)
+{
+    k_forward_batched<NV><<<grid, 32 * kBatchTileY, 0, s>>>(jobs, hdr, counter);
+    return cudaGetLastError();
+}
+
+template <int NV>
+int batched_grid_nv()
+{
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV>, 32 * kBatchTileY, 0);
+    return sms * (per > 0 ? per : 1);
+}
+
 }  // namespace
+
+cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
+                                   unsigned long long* counter, int NV, int grid,
+                                   cudaStream_t s)
+{
+    switch (NV) {
+        case 1: return launch_batched_nv<1>(jobs, hdr, counter, grid, s);
+        case 2: return launch_batched_nv<2>(jobs, hdr, counter, grid, s);
+        case 3: return launch_batched_nv<3>(jobs, hdr, counter, grid, s);
+        case 4: return launch_batched_nv<4>(jobs, hdr, counter, grid, s);
+        case 5: return launch_batched_nv<5>(jobs, hdr, counter, grid, s);
+        case 6: return launch_batched_nv<6>(jobs, hdr, counter, grid, s);
+        case 7: return launch_batched_nv<7>(jobs, hdr, counter, grid, s);
+        case 8: return launch_batched_nv<8>(jobs, hdr, counter, grid, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+int batched_grid(int NV)
+{
+    switch (NV) {
+        case 1: return batched_grid_nv<1>();
+        case 2: return batched_grid_nv<2>();
+        case 3: return batched_grid_nv<3>();
+        case 4: return batched_grid_nv<4>();
+        case 5: return batched_grid_nv<5>();
+        case 6: return batched_grid_nv<6>();
+        case 7: return batched_grid_nv<7>();
+        case 8: return batched_grid_nv<8>();
+        default: return 0;
+    }
+}
 
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s)
 {

@@ -60,6 +60,21 @@ struct VjpParams {
     int opc;             // orientations per CTA
 };
 
+// Batched pattern loop (ebsd_forward.cu): a table of jobs in device memory.
+constexpr int kBatchTileY = 8;  // CTA = 32 x 8 pixels; binning up to 8
+
+struct BatchJob {
+    FwdParams p;            // detector, master, quats, out, epilogue of the job
+    int tiles_x, ntiles, opc, pad;
+    long long item_begin;   // first work item of this job in the queue
+    long long items;        // ntiles * ceil(n / opc)
+};
+
+struct BatchHeader {
+    long long total_items;
+    int njobs, pad;
+};
+
 // Launch configuration picked by the tuner or by default.
 struct LaunchCfg {
     int tile_y = 8;        // CTA is 32 x tile_y pixels
@@ -110,5 +125,9 @@ cudaError_t launch_vjp(const FwdParams& p, const VjpParams& vp, int NV, int mode
 // Pattern kernels (ebsd_forward.cu).
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s);
 cudaError_t launch_cells(const FwdParams& p, int NV, cudaStream_t s);
+cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
+                                   unsigned long long* counter, int NV, int grid,
+                                   cudaStream_t s);
+int batched_grid(int NV);
 
 }  // namespace ebsd

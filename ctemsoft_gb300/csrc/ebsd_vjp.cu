@@ -25,48 +25,34 @@ namespace ebsd {
 
 namespace {
 
-__device__ __forceinline__ float warp_sum(float v)
+// Sum each of KP per-lane values over the warp (reduce-scatter butterfly:
+// every step halves the values a lane carries, so KP values cost about KP
+// shuffles instead of 5 KP).  On return lane l holds the warp total of value
+// index l / (32 / KP) in v[0].
+template <int KP>
+__device__ __forceinline__ void warp_reduce_scatter(float (&v)[KP], int lane)
 {
+    int off = 16;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Lambert point and its Jacobian with respect to (x, y, z), single
-// precision, reference arithmetic for the point (Lambert.f90:405-436).
-__device__ __forceinline__ void lambert_jac(float x, float y, float z, float spi2, bool accurate,
-                                            float& X, float& Y, float dX[3], float dY[3])
-{
-    lambert_inverse(x, y, z, spi2, X, Y, accurate);
-    dX[0] = dX[1] = dX[2] = 0.0f;
-    dY[0] = dY[1] = dY[2] = 0.0f;
-    const float rxy = fmaf(x, x, y * y);
-    if (!(rxy > 0.0f) || fabsf(z) >= 1.0f) return;
-    const float omz = rxy / (1.0f + z);
-    const float rho = sqrtf(2.0f * omz);
-    const float irho = 1.0f / rho, irxy = 1.0f / rxy;
-    if (fabsf(y) <= fabsf(x)) {
-        const float sg = copysignf(1.0f, x), a = atanf(y / x);
-        dX[2] = -sg * spi2 * irho;
-        const float f = sg * rho / spi2 * irxy;
-        dY[0] = -f * y;
-        dY[1] = f * x;
-        dY[2] = -sg * a * irho / spi2;
-    } else {
-        const float sg = copysignf(1.0f, y), b = atanf(x / y);
-        const float f = sg * rho / spi2 * irxy;
-        dX[0] = f * y;
-        dX[1] = -f * x;
-        dX[2] = -sg * b * irho / spi2;
-        dY[2] = -sg * spi2 * irho;
+    for (int n = KP; n > 1; n >>= 1, off >>= 1) {
+        const bool upper = (lane & off) != 0;
+#pragma unroll
+        for (int i = 0; i < n / 2; ++i) {
+            const float send = upper ? v[i] : v[i + n / 2];
+            const float keep = upper ? v[i + n / 2] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
     }
+#pragma unroll
+    for (; off > 0; off >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
 }
 
 template <int NV, int MODE>
-__global__ void __launch_bounds__(256) k_vjp(const FwdParams prm, const VjpParams vp, int tile_y,
-                                              int tiles_x, int ntiles, int opc)
+__global__ void __launch_bounds__(256, 3) k_vjp(const FwdParams prm, const VjpParams vp,
+                                                 int tile_y, int tiles_x, int ntiles, int opc)
 {
     constexpr int K = MODE == EBSD_VJP_NDP ? 15 : 6;
+    constexpr int KP = MODE == EBSD_VJP_NDP ? 16 : 8;
     extern __shared__ float sm[];  // [tile_y][33] pattern tile, then [tile_y][K] warp sums
     float* tile = sm;
     float* red = sm + 33 * tile_y;
@@ -80,18 +66,9 @@ __global__ void __launch_bounds__(256) k_vjp(const FwdParams prm, const VjpParam
     const bool inside = x < prm.numsx && y < prm.numsy && x < prm.out_nx * b &&
                         y < prm.out_ny * b;
     const int p = y * prm.numsx + x;
-    float4 r = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
-    float4 w[NV];
-#pragma unroll
-    for (int c = 0; c < NV; ++c) w[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    float4 dr[3] = {r, r, r};
-    if (inside) {
-        r = prm.rg[p];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) w[c] = prm.W[(int64_t)c * prm.P + p];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) dr[a] = vp.drg[(int64_t)a * prm.P + p];
-    }
+    // per-pixel constants (direction, weights and their derivative tables)
+    // are re-read per orientation; they are L1/L2 hits, and keeping them out
+    // of registers lets 3 CTAs share an SM without spilling
     const float pref = (float)prm.prefactor;
     const float ib2 = 1.0f / (float)(b * b);
     const int64_t rec = (int64_t)prm.out_nx * prm.out_ny;
@@ -102,6 +79,7 @@ __global__ void __launch_bounds__(256) k_vjp(const FwdParams prm, const VjpParam
         float val = 0.0f, J[6] = {0, 0, 0, 0, 0, 0};
         if (inside) {
             const float4 q = __ldg(prm.quats + o);
+            const float4 r = __ldg(prm.rg + p);
             float d0, d1, d2;
             rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
             const float nd = sqrtf(fmaf(d0, d0, fmaf(d1, d1, d2 * d2)));
@@ -110,7 +88,7 @@ __global__ void __launch_bounds__(256) k_vjp(const FwdParams prm, const VjpParam
             normalize_fold(c0, c1, c2);
             const float s = h2 < 0.0f ? -1.0f : 1.0f;
             float LX, LY, dX[3], dY[3];
-            lambert_jac(c0, c1, c2, prm.spi2, prm.accurate != 0, LX, LY, dX, dY);
+            lambert_inverse_jac(c0, c1, c2, prm.spi2, prm.accurate != 0, LX, LY, dX, dY);
             float dx, dy;
             int nix, niy;
             const int ix0 = lambert_cell(prm.scl * LX, prm.npx, dx, nix);
@@ -122,19 +100,22 @@ __global__ void __launch_bounds__(256) k_vjp(const FwdParams prm, const VjpParam
             const float4* m01 = prm.master + ((int64_t)iy1 * prm.gx + ix0) * NV;
             const float4* m11 = prm.master + ((int64_t)iy1 * prm.gx + ix1) * NV;
             float P = 0.0f, gX = 0.0f, gY = 0.0f, gW0 = 0.0f, gW1 = 0.0f, gW2 = 0.0f;
-#pragma unroll
+            // one float4 group of bins at a time: unrolling would hoist all
+            // 7*NV vector loads and spill
+#pragma unroll 1
             for (int c = 0; c < NV; ++c) {
                 const float4 A = __ldg(m00 + c), B = __ldg(m10 + c), C = __ldg(m01 + c),
                              D = __ldg(m11 + c);
+                const float4 wc = __ldg(prm.W + (int64_t)c * prm.P + p);
                 const float4 e0 = __ldg(vp.dW + (int64_t)(0 * NV + c) * prm.P + p);
                 const float4 e1 = __ldg(vp.dW + (int64_t)(1 * NV + c) * prm.P + p);
                 const float4 e2 = __ldg(vp.dW + (int64_t)(2 * NV + c) * prm.P + p);
 #define EBSD_BIN(f)                                                                        \
     {                                                                                      \
         const float bv = fmaf(A.f, dxm * dym, fmaf(B.f, dx * dym, fmaf(C.f, dxm * dy, D.f * dx * dy))); \
-        P = fmaf(w[c].f, bv, P);                                                            \
-        gX = fmaf(w[c].f, fmaf(B.f - A.f, dym, (D.f - C.f) * dy), gX);                       \
-        gY = fmaf(w[c].f, fmaf(C.f - A.f, dxm, (D.f - B.f) * dx), gY);                       \
+        P = fmaf(wc.f, bv, P);                                                              \
+        gX = fmaf(wc.f, fmaf(B.f - A.f, dym, (D.f - C.f) * dy), gX);                         \
+        gY = fmaf(wc.f, fmaf(C.f - A.f, dxm, (D.f - B.f) * dx), gY);                         \
         gW0 = fmaf(e0.f, bv, gW0);                                                          \
         gW1 = fmaf(e1.f, bv, gW1);                                                          \
         gW2 = fmaf(e2.f, bv, gW2);                                                          \
@@ -161,9 +142,11 @@ __global__ void __launch_bounds__(256) k_vjp(const FwdParams prm, const VjpParam
             const float m0 = q.x * u1 - q.y * u0 - q.z * u3 + q.w * u2;
             const float m1 = q.x * u2 + q.y * u3 - q.z * u0 - q.w * u1;
             const float m2 = q.x * u3 - q.y * u2 + q.z * u1 - q.w * u0;
-            J[3] = m0 * dr[0].x + m1 * dr[0].y + m2 * dr[0].z + pref * gW0;
-            J[4] = m0 * dr[1].x + m1 * dr[1].y + m2 * dr[1].z + pref * gW1;
-            J[5] = m0 * dr[2].x + m1 * dr[2].y + m2 * dr[2].z + pref * gW2;
+            const float4 r0 = __ldg(vp.drg + p), r1 = __ldg(vp.drg + prm.P + p),
+                         r2 = __ldg(vp.drg + 2 * (int64_t)prm.P + p);
+            J[3] = m0 * r0.x + m1 * r0.y + m2 * r0.z + pref * gW0;
+            J[4] = m0 * r1.x + m1 * r1.y + m2 * r1.z + pref * gW1;
+            J[5] = m0 * r2.x + m1 * r2.y + m2 * r2.z + pref * gW2;
         }
         // output-record value of this pixel's block
         float O = val;
@@ -179,7 +162,9 @@ __global__ void __launch_bounds__(256) k_vjp(const FwdParams prm, const VjpParam
             }
             __syncthreads();
         }
-        float acc[K];
+        float acc[KP];
+#pragma unroll
+        for (int a = K; a < KP; ++a) acc[a] = 0.0f;
         if (inside) {
             const float dv = vp.data[o * rec + (int64_t)Y * prm.out_nx + X];
             if (MODE == EBSD_VJP_NDP) {
@@ -201,10 +186,10 @@ __global__ void __launch_bounds__(256) k_vjp(const FwdParams prm, const VjpParam
 #pragma unroll
             for (int a = 0; a < K; ++a) acc[a] = 0.0f;
         }
-#pragma unroll
-        for (int a = 0; a < K; ++a) {
-            const float v = warp_sum(acc[a]);
-            if (tx == 0) red[ty * K + a] = v;
+        warp_reduce_scatter<KP>(acc, tx);
+        {
+            const int idx = tx / (32 / KP);
+            if (tx % (32 / KP) == 0 && idx < K) red[ty * K + idx] = acc[0];
         }
         __syncthreads();
         if (tid < K) {

@@ -255,6 +255,34 @@ C5 = Workload("gauss-newton-480x480-bin4-npx500", 480, 480, 20.0, 15000.0, 10.0,
               6.0, 1.0, 20.0, 15, 100000, 4, binning=4, scalingmode="lin")
 
 
+C3_SIZES = [(80, 60), (160, 120), (320, 240), (640, 480), (1244, 1024)]
+
+
+def c3_jobs(seed: int = 2, njobs: int = 64):
+    """The batched uneven workload: njobs draws of detector size (uniform
+    over C3_SIZES), binning (1, 2, 4, 8), orientation count (log-uniform in
+    [1, 5000]) and phase (Ni or Ti).  Every detector spans the 12.8 mm of
+    the 640x480 / 20 um camera (delta = 12800/numsx), L = 15000 um, tilt 10
+    deg; gamma 0.33.  Returns dicts with keys numsx, numsy, delta, binning,
+    n, phase, seed."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for j in range(njobs):
+        nx, ny = C3_SIZES[int(rng.integers(0, len(C3_SIZES)))]
+        b = int(rng.choice([1, 2, 4, 8]))
+        n = int(np.clip(np.round(np.exp(rng.uniform(0.0, np.log(5000.0)))), 1, 5000))
+        ph = "Ni" if rng.random() < 0.5 else "Ti"
+        jobs.append(dict(numsx=nx, numsy=ny, delta=12800.0 / nx, binning=b, n=n, phase=ph,
+                         seed=1000 + j))
+    return jobs
+
+
+def c3_phase(phase: str) -> Workload:
+    """Master/MC workload of one C3 phase: half-width 500, 11 bins 10-20 keV."""
+    return Workload(f"batched-{phase}-npx500", 640, 480, 20.0, 15000.0, 10.0, 0.0, 0.0, 500,
+                    10.0, 1.0, 20.0, 11, 0, 2 if phase == "Ni" else 12, phase=phase)
+
+
 def tiny(seed: int = 7, numsx: int = 24, numsy: int = 18, npx: int = 40, nE: int = 5,
          mc_nsx: int = 60, n_orient: int = 6, phase: str = "Ni") -> Workload:
     """A small workload the oracle finishes in milliseconds."""

@@ -138,6 +138,40 @@ int ebsd_output_dims(const ebsd_handle* h, const ebsd_epilogue* e, int32_t* nx, 
 int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
                  float* out);
 
+/* One job of a batch: the orientations of one detector (its handle holds
+ * the detector and, possibly shared, master) with its own epilogue. */
+typedef struct {
+    ebsd_handle* source;    /* handle with this job's master and detector */
+    const float* quats;     /* device memory, n x 4 (scalar first) */
+    int64_t n;
+    ebsd_epilogue epilogue; /* prefactor, binning 1/2/4/8, 'not'/'lin'/'gam' */
+    float* out;             /* device memory, n records of the job's output size */
+} ebsd_job;
+
+#define EBSD_BATCH_GRAPH 1 /* capture the batch in a CUDA graph and replay it */
+
+/* Launch-shape autotuner (no reference counterpart): times the pattern
+ * kernel for this handle's detector and epilogue over n_sample orientations
+ * at 128, 256 and 512 pixels per CTA x 1, 2, 4 and 8 orientations per CTA,
+ * applies the fastest, and appends it to cache_path (a text file of
+ * "shape key|tile_y|orient_per_cta|us per pattern" lines; NULL = no file).
+ * A shape already in the file is applied without timing.  Any of the
+ * outputs may be NULL. */
+int ebsd_autotune(ebsd_handle* h, const ebsd_epilogue* e, int64_t n_sample,
+                  const char* cache_path, int32_t* tile_y, int32_t* orient_per_cta,
+                  float* us_per_pattern);
+
+/* Many pattern loops of uneven size in one persistent launch (no reference
+ * counterpart: the reference runs one detector per process).  Jobs may
+ * differ in detector size, binning, epilogue, orientation count and master
+ * (phase); all sources must be on h's device.  A device work queue of
+ * (job, 32x8-pixel tile, run of orientations) items is consumed by one
+ * persistent grid (one launch per distinct energy-bin count).  With
+ * EBSD_BATCH_GRAPH the table upload, queue reset and launches are captured
+ * in a CUDA graph on first use and replayed for later batches with the same
+ * number of jobs.  Runs on h's stream; returns when the work is queued. */
+int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_t njobs, int32_t flags);
+
 /* Adjoint modes of ebsd_vjp. */
 #define EBSD_VJP_COTANGENT 0 /* data = cotangent on the output records */
 #define EBSD_VJP_NDP 1       /* data = target records; loss = 1 - normalised dot product */

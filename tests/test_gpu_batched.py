@@ -1,0 +1,114 @@
+"""Batched persistent pattern loop (ebsd_forward_batched) and the
+launch-shape autotuner, on the GPU."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from ctemsoft_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed_jobs(torch, seed=3):
+    """Jobs of different detector size, binning, epilogue, orientation count
+    and phase; detectors of one phase share that phase's master."""
+    ni = synth.tiny(seed=1, numsx=24, numsy=18, npx=40, nE=5, phase="Ni")
+    ti = synth.tiny(seed=2, numsx=24, numsy=18, npx=40, nE=5, phase="Ti")
+    masters = {}
+    for ph, wl in (("Ni", ni), ("Ti", ti)):
+        h = capi.Handle(0)
+        h.set_master(wl.master())
+        masters[ph] = (h, wl.mc())
+    rng = np.random.default_rng(seed)
+    shapes = [(80, 60), (37, 29), (160, 120), (64, 48), (320, 240), (101, 77)]
+    jobs = []
+    for j in range(10):
+        nx, ny = shapes[j % len(shapes)]
+        ph = "Ni" if j % 3 else "Ti"
+        mh, acc = masters[ph]
+        h = capi.Handle(0)
+        h.share_master(mh)
+        geom = dict(L=15000.0, thetac=10.0, delta=12800.0 / nx, numsx=nx, numsy=ny,
+                    xpc=float(rng.normal(0, 2)), ypc=float(rng.normal(0, 2)), sig=70.0)
+        num_el = h.set_detector(geom, acc, 1, 5)
+        b = [1, 2, 4, 8][j % 4]
+        mode = ["not", "lin", "gam"][j % 3]
+        n = int(rng.integers(1, 120))
+        epi = capi.epilogue(capi.prefactor(15.0, 100.0, num_el), binning=b, scalingmode=mode,
+                            gammavalue=0.33)
+        ox, oy = h.output_dims(epi)
+        q = torch.from_numpy(synth.shoemake_quaternions(n, 100 + j)).cuda()
+        out = torch.full((n, oy, ox), -1.0, device="cuda")
+        jobs.append((h, q, epi, out))
+    return masters, jobs
+
+
+def test_batched_matches_per_job_launches(built):
+    torch = pytest.importorskip("torch")
+    masters, jobs = _mixed_jobs(torch)
+    runner = jobs[0][0]
+    runner.forward_batched(jobs)
+    torch.cuda.synchronize()
+    for i, (h, q, epi, out) in enumerate(jobs):
+        ref = torch.empty_like(out)
+        h.forward(q, epi, out=ref)
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref), f"job {i}"
+
+
+def test_batched_graph_replays_new_inputs(built):
+    torch = pytest.importorskip("torch")
+    masters, jobs = _mixed_jobs(torch)
+    runner = capi.Handle(0)
+    runner.forward_batched(jobs, graph=True)
+    for rep in range(2):
+        # new orientations in the same buffers: the graph must pick them up
+        for k, (h, q, epi, out) in enumerate(jobs):
+            q.copy_(torch.from_numpy(synth.shoemake_quaternions(q.shape[0], 500 + 7 * rep + k)))
+            out.fill_(-1.0)
+        torch.cuda.synchronize()
+        runner.forward_batched(jobs, graph=True)
+        torch.cuda.synchronize()
+        for i, (h, q, epi, out) in enumerate(jobs):
+            ref = torch.empty_like(out)
+            h.forward(q, epi, out=ref)
+            torch.cuda.synchronize()
+            assert torch.equal(out, ref), f"replay {rep} job {i}"
+
+
+def test_batched_rejects_host_buffers_and_skips_empty_jobs(built):
+    torch = pytest.importorskip("torch")
+    masters, jobs = _mixed_jobs(torch)
+    h, q, epi, out = jobs[0]
+    empty = (h, q[:0], epi, out[:0])
+    h.forward_batched([empty, jobs[1]])
+    torch.cuda.synchronize()
+    with pytest.raises(capi.EBSDError) as e:
+        h.forward_batched([(h, q.cpu().numpy(), epi, out)])
+    assert e.value.code == capi.EBSD_EINVAL
+
+
+def test_autotune_and_cache(built, tmp_path):
+    wl = synth.tiny(numsx=160, numsy=120, npx=60, nE=5)
+    h = capi.Handle(0)
+    h.set_master(wl.master())
+    h.set_detector(wl.geometry(), wl.mc(), 1, 5)
+    epi = capi.epilogue(1.0, binning=4, scalingmode="lin")
+    cache = tmp_path / "tune.txt"
+    ty, oc, us = h.autotune(epi, 32, cache)
+    assert ty in (4, 8, 16) and ty % 4 == 0 and oc in (1, 2, 4, 8) and us > 0
+    lines = cache.read_text().splitlines()
+    assert len(lines) == 1 and lines[0].endswith(f"|{ty}|{oc}|{us:.4f}")
+    # a second tuner call reads the cache instead of timing
+    h2 = capi.Handle(0)
+    h2.share_master(h)
+    h2.set_detector(wl.geometry(), wl.mc(), 1, 5)
+    assert h2.autotune(epi, 32, cache)[:2] == (ty, oc)
+    assert len(cache.read_text().splitlines()) == 1
+    # the tuned shape computes the same patterns as the default one
+    q = wl.quaternions(7)
+    h3 = capi.Handle(0)
+    h3.share_master(h)
+    h3.set_detector(wl.geometry(), wl.mc(), 1, 5)
+    assert np.array_equal(h2.forward(q, epi), h3.forward(q, epi))
