@@ -35,7 +35,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"
 
 CU_SOURCES = ["ebsd_setup.cu", "ebsd_forward.cu", "ebsd_vjp.cu", "ebsd_capi.cu"]
 CXX_SOURCES = ["ebsd_host.cpp", "ebsd_program.cpp"]
-HEADERS = ["ebsd_internal.h", "ebsd_device.cuh", "ebsd_host.h"]
+HEADERS = ["ebsd_internal.h", "ebsd_device.cuh", "ebsd_host.h", "ebsd_noise.cuh"]
 
 LIBNAME = "libebsdgpu.so"
 EXE = "ctemebsd"

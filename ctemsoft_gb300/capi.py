@@ -53,6 +53,11 @@ class Job(C.Structure):
 BATCH_GRAPH = 1
 
 
+class GNOptions(C.Structure):
+    _fields_ = [("max_iterations", C.c_int32), ("refine_pc", C.c_int32), ("damping", C.c_double),
+                ("tol_rad", C.c_double), ("tol_pc", C.c_double)]
+
+
 class MCHeader(C.Structure):
     _fields_ = [("numEbins", C.c_int32), ("numzbins", C.c_int32), ("numsx", C.c_int32),
                 ("numsy", C.c_int32), ("num_el_total", C.c_int64), ("nthreads", C.c_int32),
@@ -98,6 +103,11 @@ _SIGS = {
     "ebsd_forward": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P]),
     "ebsd_cells": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P, _P]),
     "ebsd_forward_batched": (C.c_int, [_P, C.POINTER(Job), C.c_int32, C.c_int32]),
+    "ebsd_gn_accumulate": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P, C.c_double,
+                                     _P, _P]),
+    "ebsd_gn_apply": (C.c_int, [_P, _P, C.c_int64, C.c_double, _P, C.POINTER(C.c_double)]),
+    "ebsd_refine": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P, C.POINTER(GNOptions),
+                              _P, C.POINTER(Geometry), C.POINTER(C.c_int32)]),
     "ebsd_autotune": (C.c_int, [_P, C.POINTER(Epilogue), C.c_int64, C.c_char_p,
                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                 C.POINTER(C.c_float)]),
@@ -290,6 +300,37 @@ class Handle:
                          int(q.shape[0]), epi, _ptr(out))
         _check(lib().ebsd_forward_batched(self._h, arr, len(jobs), BATCH_GRAPH if graph else 0),
                self._h)
+
+    def gn_accumulate(self, quats, epi: Epilogue, targets, damping=1e-3, pc_system=False,
+                      loss=None):
+        """Phase 1 of a Gauss-Newton step (device tensors).  Returns the
+        12-number centre system (numpy) when pc_system is true."""
+        sysc = np.zeros(12) if pc_system else None
+        _check(lib().ebsd_gn_accumulate(self._h, _ptr(quats), int(quats.shape[0]), C.byref(epi),
+                                        _ptr(targets), damping, _ptr(sysc), _ptr(loss)), self._h)
+        return sysc
+
+    def gn_apply(self, quats, damping=1e-3, dpc=None):
+        """Phase 2: update quats in place; returns the largest step (rad)."""
+        d = None if dpc is None else np.ascontiguousarray(dpc, np.float64)
+        ms = C.c_double()
+        _check(lib().ebsd_gn_apply(self._h, _ptr(quats), int(quats.shape[0]), damping, _ptr(d),
+                                   C.byref(ms)), self._h)
+        return ms.value
+
+    def refine(self, quats, epi: Epilogue, targets, max_iterations=20, refine_pc=False,
+               damping=1e-3, tol_rad=1e-6, tol_pc=1e-4, loss=None):
+        """Gauss-Newton refinement on the device (quats updated in place).
+        Returns (iterations, refined geometry dict)."""
+        opt = GNOptions(max_iterations, int(refine_pc), damping, tol_rad, tol_pc)
+        g = Geometry()
+        it = C.c_int32()
+        _check(lib().ebsd_refine(self._h, _ptr(quats), int(quats.shape[0]), C.byref(epi),
+                                 _ptr(targets), C.byref(opt), _ptr(loss), C.byref(g),
+                                 C.byref(it)), self._h)
+        geom = {k: getattr(g, k) for k, _ in Geometry._fields_}
+        self.geometry = dict(geom)
+        return it.value, geom
 
     def cells(self, quats: np.ndarray):
         q = np.ascontiguousarray(quats, dtype=np.float32)

@@ -70,7 +70,12 @@ struct ebsd_handle {
     DeviceBuf quats[2];
     DeviceBuf outb[2];
     DeviceBuf tmp;
+    DeviceBuf accum;           // MC histogram, kept for geometry updates
+    DeviceBuf small;           // set-up scalars (num_el sum)
     DeviceBuf vjp_partial;     // per-CTA partial sums of the adjoint
+    DeviceBuf gn_sys;          // per-pattern Gauss-Newton systems (28 doubles)
+    DeviceBuf gn_aux;          // Schur partials, centre system, centre step, steps
+    int64_t gn_n = 0;
     DeviceBuf vjp_io;          // device copies of host quats / data / outputs
     float* pinned[2] = {nullptr, nullptr};
     size_t pinned_bytes = 0;
@@ -227,8 +232,6 @@ int fill_params(ebsd_handle* h, const ebsd_epilogue* e, FwdParams& p)
                 return set_err(h, EBSD_EINVAL, "binning %d leaves no full block on a %dx%d detector",
                                b, p.numsx, p.numsy);
         }
-        if (e->poisson)
-            return set_err(h, EBSD_EUNSUPPORTED, "Poisson noise is not available in this build");
     }
     return EBSD_OK;
 }
@@ -251,8 +254,10 @@ int check_quats_host(ebsd_handle* h, const float* q, int64_t n)
     return EBSD_OK;
 }
 
-int launch_chunk(ebsd_handle* h, FwdParams p, const float4* dq, int64_t n, float* dout)
+int launch_chunk(ebsd_handle* h, FwdParams p, const float4* dq, int64_t n, float* dout,
+                 int64_t o_offset = 0)
 {
+    p.o_offset = o_offset;
     p.quats = dq;
     p.n = n;
     p.out = dout;
@@ -322,6 +327,10 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
         if (h->ev_d2h[i]) cudaEventDestroy(h->ev_d2h[i]);
     }
     cudaFree(h->tmp.ptr);
+    cudaFree(h->accum.ptr);
+    cudaFree(h->small.ptr);
+    cudaFree(h->gn_sys.ptr);
+    cudaFree(h->gn_aux.ptr);
     cudaFree(h->batch_table.ptr);
     if (h->batch_table_host) cudaFreeHost(h->batch_table_host);
     if (h->batch_exec) cudaGraphExecDestroy(h->batch_exec);
@@ -457,6 +466,67 @@ extern "C" double ebsd_prefactor(double beamcurrent, double dwelltime, int32_t n
     return host::prefactor(beamcurrent, dwelltime, num_el);
 }
 
+namespace {
+
+// Detector tables for geometry g from the histogram already on the device
+// (h->accum): direction cosines, weights, derivative tables and, when
+// with_num_el, num_el of CTEMEBSD.f90:516.  The energy window and MC grid
+// are h's.
+int detector_setup(ebsd_handle* h, const ebsd_geometry* g, bool with_num_el)
+{
+    cudaStream_t s = h->stream;
+    CK(h, cudaStreamSynchronize(s), "detector set-up");
+    const int P = g->numsx * g->numsy;
+    const int nsel = h->Emax - h->Emin + 1;
+    const int NV = (nsel + 3) / 4;
+    if (P != h->P || NV != h->NV || !h->d_rg) {
+        cudaFree(h->d_rg);
+        cudaFree(h->d_W);
+        cudaFree(h->d_drg);
+        cudaFree(h->d_dW);
+        h->d_rg = nullptr;
+        h->d_W = nullptr;
+        h->d_drg = nullptr;
+        h->d_dW = nullptr;
+        h->P = 0;
+        CK(h, cudaMalloc(&h->d_rg, sizeof(float4) * (size_t)P), "cudaMalloc rg");
+        CK(h, cudaMalloc(&h->d_W, sizeof(float4) * (size_t)P * NV), "cudaMalloc W");
+        CK(h, cudaMalloc(&h->d_drg, sizeof(float4) * (size_t)P * 3), "cudaMalloc drg");
+        CK(h, cudaMalloc(&h->d_dW, sizeof(float4) * (size_t)P * 3 * NV), "cudaMalloc dW");
+    }
+    const int32_t* acc = (const int32_t*)h->accum.ptr;
+    float ca, sa;
+    host::detector_angles(g->sig, g->thetac, &ca, &sa);
+    CK(h, launch_detector(*g, ca, sa, h->d_rg, s), "detector kernel");
+    const float sclmc = host::lambert_scale(h->nsx);
+    float4* d_wref = nullptr;
+    CK(h, cudaMalloc(&d_wref, sizeof(float4) * (size_t)P * NV), "cudaMalloc weights");
+    cudaError_t e = launch_weights(h->d_rg, P, acc, h->nE, h->nsx, h->nsy, sclmc,
+                                   host::lambert_spi2_f(), h->Emin - 1, nsel, NV,
+                                   h->weights_fp64, *g, h->d_W, d_wref, s);
+    if (e == cudaSuccess)
+        e = launch_geom_derivs(*g, acc, h->nE, h->nsx, h->nsy, h->Emin - 1, nsel, NV, h->d_drg,
+                               h->d_dW, s);
+    float sum = 0.0f;
+    if (with_num_el) {
+        float* d_sum = (float*)h->small.ptr;
+        if (e == cudaSuccess) e = launch_num_el(d_wref, P, nsel, NV, d_sum, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&sum, d_sum, sizeof(float), cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d_wref);
+    if (e != cudaSuccess) return cuda_err(h, e, "detector weights");
+    if (with_num_el) h->num_el = (int32_t)lroundf(sum);
+    h->geom = *g;
+    h->P = P;
+    h->NV = NV;
+    h->nsel = nsel;
+    return EBSD_OK;
+}
+
+}  // namespace
+
 extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const int32_t* accum_e,
                                  int32_t nsx, int32_t nsy, int32_t numEbins, int32_t Emin,
                                  int32_t Emax, int32_t* num_el)
@@ -483,22 +553,8 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
     cudaStream_t s = h->stream;
     cudaStreamSynchronize(s);
     h->have_detector = false;
-
-    const int P = g->numsx * g->numsy;
     const int nsel = Emax - Emin + 1;
     const int NV = (nsel + 3) / 4;
-    cudaFree(h->d_rg);
-    cudaFree(h->d_W);
-    cudaFree(h->d_drg);
-    cudaFree(h->d_dW);
-    h->d_rg = nullptr;
-    h->d_W = nullptr;
-    h->d_drg = nullptr;
-    h->d_dW = nullptr;
-    CK(h, cudaMalloc(&h->d_rg, sizeof(float4) * (size_t)P), "cudaMalloc rg");
-    CK(h, cudaMalloc(&h->d_W, sizeof(float4) * (size_t)P * NV), "cudaMalloc W");
-    CK(h, cudaMalloc(&h->d_drg, sizeof(float4) * (size_t)P * 3), "cudaMalloc drg");
-    CK(h, cudaMalloc(&h->d_dW, sizeof(float4) * (size_t)P * 3 * NV), "cudaMalloc dW");
 
     // master re-layout for this window
     {
@@ -521,44 +577,21 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
         h->il_bytes = it->second.second;
     }
 
-    float ca, sa;
-    host::detector_angles(g->sig, g->thetac, &ca, &sa);
-    CK(h, launch_detector(*g, ca, sa, h->d_rg, s), "detector kernel");
-
+    // the histogram stays on the device for later geometry updates
     const size_t acc_bytes = sizeof(int32_t) * (size_t)numEbins * (2 * nsx + 1) * (2 * nsy + 1);
-    rc = ensure(h, h->tmp, std::max(acc_bytes, sizeof(float) * 4), "MC histogram");
+    rc = ensure(h, h->accum, acc_bytes, "MC histogram");
     if (rc) return rc;
-    CK(h, cudaMemcpyAsync(h->tmp.ptr, accum_e, acc_bytes, cudaMemcpyHostToDevice, s),
+    rc = ensure(h, h->small, 256, "set-up scalars");
+    if (rc) return rc;
+    CK(h, cudaMemcpyAsync(h->accum.ptr, accum_e, acc_bytes, cudaMemcpyHostToDevice, s),
        "MC upload");
-    const float sclmc = host::lambert_scale(nsx);
-    float4* d_wref = nullptr;
-    CK(h, cudaMalloc(&d_wref, sizeof(float4) * (size_t)P * NV), "cudaMalloc weights");
-    cudaError_t e = launch_weights(h->d_rg, P, (const int32_t*)h->tmp.ptr, numEbins, nsx, nsy,
-                                   sclmc, host::lambert_spi2_f(), Emin - 1, nsel, NV,
-                                   h->weights_fp64, *g, h->d_W, d_wref, s);
-    if (e == cudaSuccess)
-        e = launch_geom_derivs(*g, (const int32_t*)h->tmp.ptr, numEbins, nsx, nsy, Emin - 1, nsel,
-                               NV, h->d_drg, h->d_dW, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    // num_el reuses the start of the histogram buffer, after the weights ran
-    float* d_sum = (float*)h->tmp.ptr;
-    if (e == cudaSuccess) e = launch_num_el(d_wref, P, nsel, NV, d_sum, s);
-    float sum = 0.0f;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&sum, d_sum, sizeof(float), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFree(d_wref);
-    if (e != cudaSuccess) return cuda_err(h, e, "detector weights");
-    h->num_el = (int32_t)lroundf(sum);
-    if (num_el) *num_el = h->num_el;
-
-    h->geom = *g;
     h->Emin = Emin;
     h->Emax = Emax;
-    h->nsel = nsel;
-    h->NV = NV;
-    h->P = P;
     h->nsx = nsx;
     h->nsy = nsy;
+    rc = detector_setup(h, g, true);
+    if (rc) return rc;
+    if (num_el) *num_el = h->num_el;
 
     // keep the master resident in L2 for the pattern kernels: a persisting
     // carve-out (a limit of this process's context) and an access-policy
@@ -682,7 +715,7 @@ extern "C" int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const
                "quaternion upload");
             dq = (const float4*)h->quats[b].ptr;
         }
-        rc = launch_chunk(h, p, dq, m, (float*)h->outb[b].ptr);
+        rc = launch_chunk(h, p, dq, m, (float*)h->outb[b].ptr, o0);
         if (rc) return rc;
         CK(h, cudaEventRecord(h->ev_comp[b], s), "event");
         CK(h, cudaStreamWaitEvent(h->copy_stream, h->ev_comp[b], 0), "wait");
@@ -910,6 +943,185 @@ extern "C" int ebsd_vjp_noalloc(ebsd_handle* h, const float* quats, int64_t n,
     return EBSD_OK;
 }
 
+
+// ----------------------------------------------------------------------
+// Gauss-Newton refinement
+
+namespace {
+
+int gn_check(ebsd_handle* h, const ebsd_epilogue* e, const float* quats, const float* targets)
+{
+    if (!e || !quats || !targets) return set_err(h, EBSD_EINVAL, "Gauss-Newton: null argument");
+    if (e->scalingmode == EBSD_SCALING_GAM || e->poisson)
+        return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: gamma and noise have no adjoint");
+    if (h->NV > 8) return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: at most 32 energy bins");
+    if (ptr_kind(quats) != kDevice || ptr_kind(targets) != kDevice)
+        return set_err(h, EBSD_EINVAL, "Gauss-Newton: quats and targets must be device memory");
+    return EBSD_OK;
+}
+
+}  // namespace
+
+extern "C" int ebsd_gn_accumulate(ebsd_handle* h, const float* quats, int64_t n,
+                                  const ebsd_epilogue* e, const float* targets, double damping,
+                                  double* pc_system, float* loss)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n < 1) return set_err(h, EBSD_EINVAL, "ebsd_gn_accumulate: no orientations");
+    rc = gn_check(h, e, quats, targets);
+    if (rc) return rc;
+    if (loss && ptr_kind(loss) != kDevice)
+        return set_err(h, EBSD_EINVAL, "ebsd_gn_accumulate: loss must be device memory");
+    rc = activate(h);
+    if (rc) return rc;
+    FwdParams p;
+    rc = fill_params(h, e, p);
+    if (rc) return rc;
+    VjpParams vp;
+    memset(&vp, 0, sizeof vp);
+    vp.drg = h->d_drg;
+    vp.dW = h->d_dW;
+    vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
+    vp.opc = 2;
+    const int tile_y = 8;
+    if (vp.binning > tile_y)
+        return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: binning %d exceeds the tile",
+                       vp.binning);
+    const int ntiles = vjp_tiles(p, tile_y);
+    const size_t rec = (size_t)p.out_nx * p.out_ny;
+    const size_t per_o = (size_t)ntiles * kGnPartialK * sizeof(float);
+    int64_t chunk = (int64_t)std::max<size_t>(1, (size_t(512) << 20) / per_o);
+    chunk = std::min<int64_t>(chunk, n);
+    rc = ensure(h, h->vjp_partial, (size_t)chunk * per_o, "Gauss-Newton partials");
+    if (rc) return rc;
+    rc = ensure(h, h->gn_sys, sizeof(double) * kGnSysK * (size_t)n, "Gauss-Newton systems");
+    if (rc) return rc;
+    const int nb = gn_schur_blocks(n);
+    const size_t aux = sizeof(double) * (12 * (size_t)nb + 12 + 4) + sizeof(float) * (size_t)n;
+    rc = ensure(h, h->gn_aux, aux, "Gauss-Newton scratch");
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    double* sys = (double*)h->gn_sys.ptr;
+    for (int64_t o0 = 0; o0 < n; o0 += chunk) {
+        const int64_t m = std::min<int64_t>(chunk, n - o0);
+        p.n = m;
+        p.quats = (const float4*)quats + o0;
+        vp.data = targets + (size_t)o0 * rec;
+        vp.partial = (float*)h->vjp_partial.ptr;
+        cudaError_t ce = launch_gn_accumulate(p, vp, h->NV, tile_y, sys + kGnSysK * o0,
+                                              loss ? loss + o0 : nullptr, s);
+        if (ce != cudaSuccess) return cuda_err(h, ce, "Gauss-Newton accumulate");
+    }
+    h->gn_n = n;
+    if (pc_system) {
+        double* partial = (double*)h->gn_aux.ptr;
+        double* out = partial + 12 * (size_t)nb;
+        CK(h, launch_gn_schur(sys, n, damping, partial, out, s), "Gauss-Newton centre system");
+        CK(h, cudaMemcpyAsync(pc_system, out, 12 * sizeof(double), cudaMemcpyDeviceToHost, s),
+           "centre system copy");
+        CK(h, cudaStreamSynchronize(s), "Gauss-Newton accumulate");
+    }
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_gn_apply(ebsd_handle* h, float* quats, int64_t n, double damping,
+                             const double* dpc, double* max_step)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n != h->gn_n || n < 1)
+        return set_err(h, EBSD_ESTATE, "ebsd_gn_apply: %lld orientations, the last accumulate "
+                       "had %lld", (long long)n, (long long)h->gn_n);
+    if (!quats || ptr_kind(quats) != kDevice)
+        return set_err(h, EBSD_EINVAL, "ebsd_gn_apply: quats must be device memory");
+    rc = activate(h);
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    const int nb = gn_schur_blocks(n);
+    double* d_dpc = (double*)h->gn_aux.ptr + 12 * (size_t)nb + 12;
+    float* steps = (float*)(d_dpc + 4);
+    if (dpc) CK(h, cudaMemcpyAsync(d_dpc, dpc, 3 * sizeof(double), cudaMemcpyHostToDevice, s),
+                "centre step upload");
+    CK(h, launch_gn_update((const double*)h->gn_sys.ptr, n, damping, dpc ? d_dpc : nullptr,
+                           (float4*)quats, steps, s),
+       "Gauss-Newton update");
+    if (max_step) {
+        std::vector<float> st((size_t)n);
+        CK(h, cudaMemcpyAsync(st.data(), steps, sizeof(float) * n, cudaMemcpyDeviceToHost, s),
+           "step copy");
+        CK(h, cudaStreamSynchronize(s), "Gauss-Newton apply");
+        double mx = 0.0;
+        for (float v : st) mx = std::max(mx, (double)v);
+        *max_step = mx;
+    }
+    return EBSD_OK;
+}
+
+// Solve the damped 3x3 centre system (S + lambda diag S) d = r.
+static bool solve3(const double S[9], const double r[3], double lambda, double d[3])
+{
+    double A[9];
+    memcpy(A, S, sizeof A);
+    for (int i = 0; i < 3; ++i) A[i * 4] *= 1.0 + lambda;
+    const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8],
+                 c02 = A[3] * A[7] - A[4] * A[6];
+    const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+    if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) return false;
+    const double inv[9] = {c00, A[2] * A[7] - A[1] * A[8], A[1] * A[5] - A[2] * A[4],
+                           c01, A[0] * A[8] - A[2] * A[6], A[2] * A[3] - A[0] * A[5],
+                           c02, A[1] * A[6] - A[0] * A[7], A[0] * A[4] - A[1] * A[3]};
+    for (int i = 0; i < 3; ++i)
+        d[i] = (inv[i * 3] * r[0] + inv[i * 3 + 1] * r[1] + inv[i * 3 + 2] * r[2]) / det;
+    return true;
+}
+
+extern "C" int ebsd_refine(ebsd_handle* h, float* quats, int64_t n, const ebsd_epilogue* e,
+                           const float* targets, const ebsd_gn_options* opt, float* loss,
+                           ebsd_geometry* geom, int32_t* iterations)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (!opt || opt->max_iterations < 0) return set_err(h, EBSD_EINVAL, "ebsd_refine: options");
+    if (opt->refine_pc && !geom)
+        return set_err(h, EBSD_EINVAL, "ebsd_refine: refine_pc needs the geometry argument");
+    int it = 0;
+    ebsd_geometry g = h->geom;
+    for (; it < opt->max_iterations; ++it) {
+        double sysc[12];
+        rc = ebsd_gn_accumulate(h, quats, n, e, targets, opt->damping,
+                                opt->refine_pc ? sysc : nullptr, loss);
+        if (rc) return rc;
+        double dpc[3] = {0.0, 0.0, 0.0};
+        if (opt->refine_pc && !solve3(sysc, sysc + 9, opt->damping, dpc))
+            dpc[0] = dpc[1] = dpc[2] = 0.0;
+        double mstep = 0.0;
+        rc = ebsd_gn_apply(h, quats, n, opt->damping, opt->refine_pc ? dpc : nullptr, &mstep);
+        if (rc) return rc;
+        const double pcstep = std::max(std::fabs(dpc[0]), std::max(std::fabs(dpc[1]),
+                                                                   std::fabs(dpc[2])));
+        if (opt->refine_pc && pcstep > 0.0) {
+            g.xpc = (float)((double)g.xpc + dpc[0]);
+            g.ypc = (float)((double)g.ypc + dpc[1]);
+            g.L = (float)((double)g.L + dpc[2]);
+            rc = detector_setup(h, &g, false);
+            if (rc) return rc;
+        }
+        if (mstep < opt->tol_rad && (!opt->refine_pc || pcstep < opt->tol_pc)) {
+            ++it;
+            break;
+        }
+    }
+    if (loss) {  // loss at the final estimate
+        rc = ebsd_gn_accumulate(h, quats, n, e, targets, opt->damping, nullptr, loss);
+        if (rc) return rc;
+        CK(h, cudaStreamSynchronize(h->stream), "refine");
+    }
+    if (geom) *geom = h->geom;
+    if (iterations) *iterations = it;
+    return EBSD_OK;
+}
+
 // ----------------------------------------------------------------------
 // Batched pattern loop
 
@@ -917,6 +1129,7 @@ namespace {
 
 struct BatchGroup {
     int NV;
+    bool noise;
     std::vector<BatchJob> jobs;
 };
 
@@ -955,19 +1168,22 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         b.p.n = J.n;
         b.tiles_x = (b.p.numsx + kTileX - 1) / kTileX;
         b.ntiles = b.tiles_x * ((b.p.numsy + kBatchTileY - 1) / kBatchTileY);
-        b.opc = std::max(1, src->cfg.orient_per_cta);
+        b.opc = std::max(4, src->cfg.orient_per_cta);  // items of >= 4 orientations
         b.items = (long long)b.ntiles * ((J.n + b.opc - 1) / b.opc);
-        auto g = std::find_if(groups.begin(), groups.end(),
-                              [&](const BatchGroup& x) { return x.NV == src->NV; });
+        const bool noise = J.epilogue.poisson != 0;
+        auto g = std::find_if(groups.begin(), groups.end(), [&](const BatchGroup& x) {
+            return x.NV == src->NV && x.noise == noise;
+        });
         if (g == groups.end()) {
-            groups.push_back({src->NV, {}});
+            groups.push_back({src->NV, noise, {}});
             g = groups.end() - 1;
         }
         g->jobs.push_back(b);
     }
     if (groups.empty()) return EBSD_OK;
-    std::sort(groups.begin(), groups.end(),
-              [](const BatchGroup& a, const BatchGroup& b) { return a.NV < b.NV; });
+    std::sort(groups.begin(), groups.end(), [](const BatchGroup& a, const BatchGroup& b) {
+        return a.NV != b.NV ? a.NV < b.NV : a.noise < b.noise;
+    });
 
     // table: [headers][counters][jobs of group 0][jobs of group 1]...
     const size_t G = groups.size();
@@ -982,7 +1198,7 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
     CK(h, cudaStreamSynchronize(h->stream), "batch");
     std::vector<int> key;
     for (auto& g : groups) {
-        key.push_back(g.NV);
+        key.push_back(g.NV * 2 + (g.noise ? 1 : 0));
         key.push_back((int)g.jobs.size());
     }
     const bool use_graph = (flags & EBSD_BATCH_GRAPH) != 0;
@@ -1023,8 +1239,10 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         memcpy(ht + gi * sizeof(BatchHeader), &hd, sizeof hd);
         memcpy(ht + job_off + jo * sizeof(BatchJob), g.jobs.data(), g.jobs.size() * sizeof(BatchJob));
         jo += g.jobs.size();
-        auto it = h->batch_grid.find(g.NV);
-        if (it == h->batch_grid.end()) it = h->batch_grid.emplace(g.NV, batched_grid(g.NV)).first;
+        const int gk = g.NV * 2 + (g.noise ? 1 : 0);
+        auto it = h->batch_grid.find(gk);
+        if (it == h->batch_grid.end())
+            it = h->batch_grid.emplace(gk, batched_grid(g.NV, g.noise)).first;
         grids[gi] = it->second;
     }
     cudaStream_t s = h->stream;
@@ -1037,7 +1255,8 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
             e = launch_forward_batched(
                 (const BatchJob*)(dt + job_off + j0 * sizeof(BatchJob)),
                 (const BatchHeader*)(dt + gi * sizeof(BatchHeader)),
-                (unsigned long long*)(dt + cnt_off) + gi, groups[gi].NV, grids[gi], s);
+                (unsigned long long*)(dt + cnt_off) + gi, groups[gi].NV, groups[gi].noise,
+                grids[gi], s);
             j0 += groups[gi].jobs.size();
         }
         return e;

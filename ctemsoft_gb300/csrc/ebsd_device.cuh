@@ -12,6 +12,26 @@
 
 namespace ebsd {
 
+// L2 eviction priorities for loads (PTX createpolicy / L2::cache_hint): the
+// master pattern and the per-pixel detector tables are re-read by every
+// orientation, so they are fetched with evict_last and outlive the
+// streaming pattern stores (which are written evict-first).
+__device__ __forceinline__ uint64_t l2_policy_evict_last()
+{
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+__device__ __forceinline__ float4 ldg4_keep(const float4* p, uint64_t pol)
+{
+    float4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
+
 // qq3 = q (x) (0,r) (x) conjg(q), quaternions.f90:255-264,306-313 as used at
 // CTEMEBSD.f90:577-586; returns the vector part.
 __device__ __forceinline__ void rotate_direction(const float4 q, float rx, float ry, float rz,

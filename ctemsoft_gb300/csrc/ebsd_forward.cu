@@ -16,6 +16,7 @@
 // :636 and powf for 'gam'.  Only atanf and powf are CUDA's own.
 #include "ebsd_device.cuh"
 #include "ebsd_internal.h"
+#include "ebsd_noise.cuh"
 
 namespace ebsd {
 
@@ -33,7 +34,7 @@ __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 template <int NV, bool STRICT>
 __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master, int gx,
                                               int ix0, int iy0, int ix1, int iy1, float dx,
-                                              float dy, const float4 (&w)[NV])
+                                              float dy, const float4 (&w)[NV], uint64_t pol)
 {
     const float dxm = 1.0f - dx, dym = 1.0f - dy;
     const float4* m00 = master + ((int64_t)iy0 * gx + ix0) * NV;
@@ -44,8 +45,8 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
         float acc = 0.0f;
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
-            const float4 a = ldg4(m00 + c), b = ldg4(m10 + c), e = ldg4(m01 + c),
-                         f = ldg4(m11 + c);
+            const float4 a = ldg4_keep(m00 + c, pol), b = ldg4_keep(m10 + c, pol),
+                         e = ldg4_keep(m01 + c, pol), f = ldg4_keep(m11 + c, pol);
             acc = acc + w[c].x * (a.x * dxm * dym + b.x * dx * dym + e.x * dxm * dy + f.x * dx * dy);
             acc = acc + w[c].y * (a.y * dxm * dym + b.y * dx * dym + e.y * dxm * dy + f.y * dx * dy);
             acc = acc + w[c].z * (a.z * dxm * dym + b.z * dx * dym + e.z * dxm * dy + f.z * dx * dy);
@@ -56,7 +57,8 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
     float c00 = 0.0f, c10 = 0.0f, c01 = 0.0f, c11 = 0.0f;
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
-        const float4 a = ldg4(m00 + c), b = ldg4(m10 + c), e = ldg4(m01 + c), f = ldg4(m11 + c);
+        const float4 a = ldg4_keep(m00 + c, pol), b = ldg4_keep(m10 + c, pol),
+                     e = ldg4_keep(m01 + c, pol), f = ldg4_keep(m11 + c, pol);
         c00 = fmaf(w[c].x, a.x, fmaf(w[c].y, a.y, fmaf(w[c].z, a.z, fmaf(w[c].w, a.w, c00))));
         c10 = fmaf(w[c].x, b.x, fmaf(w[c].y, b.y, fmaf(w[c].z, b.z, fmaf(w[c].w, b.w, c10))));
         c01 = fmaf(w[c].x, e.x, fmaf(w[c].y, e.y, fmaf(w[c].z, e.z, fmaf(w[c].w, e.w, c01))));
@@ -82,7 +84,7 @@ __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, fl
 
 // One work item: the 32 x tile_y pixels of tile t for orientations
 // [o_begin, o_begin + opc).  `tile` is shared scratch of tile_y x 33 floats.
-template <int NV, bool STRICT>
+template <int NV, bool STRICT, bool NOISE>
 __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, int tiles_x, int t,
                                              int64_t o_begin, int opc, float* tile)
 {
@@ -93,14 +95,15 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
     const bool inside = x < prm.numsx && y < prm.numsy;
     const int p = y * prm.numsx + x;
 
+    const uint64_t pol = l2_policy_evict_last();
     float4 r = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
     float4 w[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) w[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (inside) {
-        r = prm.rg[p];
+        r = ldg4_keep(prm.rg + p, pol);
 #pragma unroll
-        for (int c = 0; c < NV; ++c) w[c] = prm.W[(int64_t)c * prm.P + p];
+        for (int c = 0; c < NV; ++c) w[c] = ldg4_keep(prm.W + (int64_t)c * prm.P + p, pol);
     }
     const bool binned = prm.mode != EBSD_SCALING_NOT && prm.binning > 1;
     const int64_t rec = (int64_t)prm.out_nx * prm.out_ny;
@@ -119,8 +122,12 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
             const int iy0 = lambert_cell(ixy1, prm.npy, dy, niy);
             const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
             const float acc =
-                gather_pixel<NV, STRICT>(prm.master, prm.gx, ix0, iy0, ix1, iy1, dx, dy, w);
+                gather_pixel<NV, STRICT>(prm.master, prm.gx, ix0, iy0, ix1, iy1, dx, dy, w, pol);
             val = (float)(prm.prefactor * (double)acc);                      // :608
+            if (NOISE) {                                                     // :611-615
+                PixelRng rng(prm.seed, (uint64_t)(prm.o_offset + o), (uint32_t)p);
+                val = poisson_draw(val, rng);
+            }
         }
         if (!binned) {
             if (prm.mode == EBSD_SCALING_GAM) val = powf(val, prm.gammavalue);  // :647-649
@@ -146,14 +153,14 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
     }
 }
 
-template <int NV, bool STRICT>
+template <int NV, bool STRICT, bool NOISE>
 __global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y, int tiles_x,
                                                  int ntiles, int opc)
 {
     extern __shared__ float tile[];  // [tile_y][33], binning only
     const int t = (int)(blockIdx.x % (unsigned)ntiles);
     const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
-    forward_tile<NV, STRICT>(prm, tile_y, tiles_x, t, o_begin, opc, tile);
+    forward_tile<NV, STRICT, NOISE>(prm, tile_y, tiles_x, t, o_begin, opc, tile);
 }
 
 // Batched pattern loop: one persistent grid works through a queue of work
@@ -161,40 +168,51 @@ __global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y
 // detectors, binnings and masters.  Each CTA takes the next item with one
 // atomic increment and stops when the queue is exhausted -- no CTA waits
 // on another, so nothing can spin.  Jobs are ordered by item_begin.
-template <int NV>
+template <int NV, bool NOISE>
 __global__ void __launch_bounds__(256) k_forward_batched(const BatchJob* __restrict__ jobs,
                                                          const BatchHeader* __restrict__ hdr,
                                                          unsigned long long* __restrict__ counter)
 {
     __shared__ float tile[kBatchTileY * 33];
-    __shared__ long long s_item;
-    __shared__ int s_job;
+    __shared__ long long s_begin[kBatchMaxJobsSmem];  // item_begin of each job
+    __shared__ long long s_item[2];
+    __shared__ int s_job[2];
     const int njobs = hdr->njobs;
     const long long total = hdr->total_items;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            const long long it = (long long)atomicAdd(counter, 1ULL);
-            s_item = it;
-            if (it < total) {
-                int lo = 0, hi = njobs - 1;  // last job with item_begin <= it
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (jobs[mid].item_begin <= it)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-                s_job = lo;
+    const bool cached = njobs <= kBatchMaxJobsSmem;
+    if (cached)
+        for (int j = threadIdx.x; j < njobs; j += blockDim.x) s_begin[j] = jobs[j].item_begin;
+    __syncthreads();
+    // thread 0 claims items one ahead: while the CTA computes item k, the
+    // claim and job lookup of item k+1 are already in flight
+    auto claim = [&](int slot) {
+        const long long it = (long long)atomicAdd(counter, 1ULL);
+        s_item[slot] = it;
+        if (it < total) {
+            int lo = 0, hi = njobs - 1;  // last job with item_begin <= it
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                const long long b = cached ? s_begin[mid] : jobs[mid].item_begin;
+                if (b <= it)
+                    lo = mid;
+                else
+                    hi = mid - 1;
             }
+            s_job[slot] = lo;
         }
-        __syncthreads();
-        const long long it = s_item;
+    };
+    if (threadIdx.x == 0) claim(0);
+    __syncthreads();
+    for (int slot = 0;; slot ^= 1) {
+        const long long it = s_item[slot];
         if (it >= total) break;
-        const BatchJob& J = jobs[s_job];
+        const int job = s_job[slot];
+        if (threadIdx.x == 0) claim(slot ^ 1);
+        const BatchJob& J = jobs[job];
         const long long local = it - J.item_begin;
         const int t = (int)(local % J.ntiles);
         const int64_t o_begin = (int64_t)(local / J.ntiles) * J.opc;
-        forward_tile<NV, false>(J.p, kBatchTileY, J.tiles_x, t, o_begin, J.opc, tile);
+        forward_tile<NV, false, NOISE>(J.p, kBatchTileY, J.tiles_x, t, o_begin, J.opc, tile);
         __syncthreads();
     }
 }
@@ -219,7 +237,7 @@ __global__ void k_cells(const FwdParams prm)
     prm.ixy1[idx] = ixy1;
 }
 
-template <int NV, bool STRICT>
+template <int NV, bool STRICT, bool NOISE>
 cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
     const int tile_y = cfg.tile_y;
@@ -237,63 +255,73 @@ cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
     lc.stream = s;
     cudaLaunchAttribute attr[1];
     set_persist_attr(cfg, attr, lc);
-    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT>, p, tile_y, tiles_x, ntiles, opc);
+    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE>, p, tile_y, tiles_x, ntiles, opc);
 }
 
 template <int NV>
 cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
-    return cfg.strict ? launch_nv2<NV, true>(p, cfg, s) : launch_nv2<NV, false>(p, cfg, s);
+    if (p.poisson) return launch_nv2<NV, false, true>(p, cfg, s);  // noise: fused gather
+    return cfg.strict ? launch_nv2<NV, true, false>(p, cfg, s)
+                      : launch_nv2<NV, false, false>(p, cfg, s);
 }
 
 template <int NV>
 cudaError_t launch_batched_nv(const BatchJob* jobs, const BatchHeader* hdr,
-                              unsigned long long* counter, int grid, cudaStream_t s)
+                              unsigned long long* counter, int grid, bool noise, cudaStream_t s)
 {
-    k_forward_batched<NV><<<grid, 32 * kBatchTileY, 0, s>>>(jobs, hdr, counter);
+    if (noise)
+        k_forward_batched<NV, true><<<grid, 32 * kBatchTileY, 0, s>>>(jobs, hdr, counter);
+    else
+        k_forward_batched<NV, false><<<grid, 32 * kBatchTileY, 0, s>>>(jobs, hdr, counter);
     return cudaGetLastError();
 }
 
 template <int NV>
-int batched_grid_nv()
+int batched_grid_nv(bool noise)
 {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV>, 32 * kBatchTileY, 0);
+    if (noise)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV, true>,
+                                                      32 * kBatchTileY, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV, false>,
+                                                      32 * kBatchTileY, 0);
     return sms * (per > 0 ? per : 1);
 }
 
 }  // namespace
 
 cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
-                                   unsigned long long* counter, int NV, int grid,
+                                   unsigned long long* counter, int NV, bool noise, int grid,
                                    cudaStream_t s)
 {
     switch (NV) {
-        case 1: return launch_batched_nv<1>(jobs, hdr, counter, grid, s);
-        case 2: return launch_batched_nv<2>(jobs, hdr, counter, grid, s);
-        case 3: return launch_batched_nv<3>(jobs, hdr, counter, grid, s);
-        case 4: return launch_batched_nv<4>(jobs, hdr, counter, grid, s);
-        case 5: return launch_batched_nv<5>(jobs, hdr, counter, grid, s);
-        case 6: return launch_batched_nv<6>(jobs, hdr, counter, grid, s);
-        case 7: return launch_batched_nv<7>(jobs, hdr, counter, grid, s);
-        case 8: return launch_batched_nv<8>(jobs, hdr, counter, grid, s);
+        case 1: return launch_batched_nv<1>(jobs, hdr, counter, grid, noise, s);
+        case 2: return launch_batched_nv<2>(jobs, hdr, counter, grid, noise, s);
+        case 3: return launch_batched_nv<3>(jobs, hdr, counter, grid, noise, s);
+        case 4: return launch_batched_nv<4>(jobs, hdr, counter, grid, noise, s);
+        case 5: return launch_batched_nv<5>(jobs, hdr, counter, grid, noise, s);
+        case 6: return launch_batched_nv<6>(jobs, hdr, counter, grid, noise, s);
+        case 7: return launch_batched_nv<7>(jobs, hdr, counter, grid, noise, s);
+        case 8: return launch_batched_nv<8>(jobs, hdr, counter, grid, noise, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
-int batched_grid(int NV)
+int batched_grid(int NV, bool noise)
 {
     switch (NV) {
-        case 1: return batched_grid_nv<1>();
-        case 2: return batched_grid_nv<2>();
-        case 3: return batched_grid_nv<3>();
-        case 4: return batched_grid_nv<4>();
-        case 5: return batched_grid_nv<5>();
-        case 6: return batched_grid_nv<6>();
-        case 7: return batched_grid_nv<7>();
-        case 8: return batched_grid_nv<8>();
+        case 1: return batched_grid_nv<1>(noise);
+        case 2: return batched_grid_nv<2>(noise);
+        case 3: return batched_grid_nv<3>(noise);
+        case 4: return batched_grid_nv<4>(noise);
+        case 5: return batched_grid_nv<5>(noise);
+        case 6: return batched_grid_nv<6>(noise);
+        case 7: return batched_grid_nv<7>(noise);
+        case 8: return batched_grid_nv<8>(noise);
         default: return 0;
     }
 }

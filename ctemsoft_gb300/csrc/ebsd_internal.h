@@ -39,6 +39,7 @@ struct FwdParams {
     int out_nx, out_ny;
     int poisson;
     uint64_t seed;
+    int64_t o_offset;      // index of quats[0] within the call (noise streams)
     int accurate;          // cancellation-free 1 - z near the poles
     // diagnostics (cells mode)
     int32_t* nix;
@@ -62,6 +63,7 @@ struct VjpParams {
 
 // Batched pattern loop (ebsd_forward.cu): a table of jobs in device memory.
 constexpr int kBatchTileY = 8;  // CTA = 32 x 8 pixels; binning up to 8
+constexpr int kBatchMaxJobsSmem = 512;  // job starts cached in shared memory
 
 struct BatchJob {
     FwdParams p;            // detector, master, quats, out, epilogue of the job
@@ -122,12 +124,23 @@ int vjp_tiles(const FwdParams& p, int tile_y);
 cudaError_t launch_vjp(const FwdParams& p, const VjpParams& vp, int NV, int mode, int tile_y,
                        cudaStream_t s);
 
+// Gauss-Newton (ebsd_vjp.cu): sys holds 28 doubles per pattern.
+constexpr int kGnPartialK = 36;
+constexpr int kGnSysK = 28;
+cudaError_t launch_gn_accumulate(const FwdParams& p, const VjpParams& vp, int NV, int tile_y,
+                                 double* sys, float* loss, cudaStream_t s);
+int gn_schur_blocks(int64_t n);
+cudaError_t launch_gn_schur(const double* sys, int64_t n, double lambda, double* partial,
+                            double* out, cudaStream_t s);
+cudaError_t launch_gn_update(const double* sys, int64_t n, double lambda, const double* dpc,
+                             float4* quats, float* step, cudaStream_t s);
+
 // Pattern kernels (ebsd_forward.cu).
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s);
 cudaError_t launch_cells(const FwdParams& p, int NV, cudaStream_t s);
 cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
-                                   unsigned long long* counter, int NV, int grid,
+                                   unsigned long long* counter, int NV, bool noise, int grid,
                                    cudaStream_t s);
-int batched_grid(int NV);
+int batched_grid(int NV, bool noise);
 
 }  // namespace ebsd

@@ -1,0 +1,117 @@
+// Poisson noise for the pattern epilogue (the step of CTEMEBSD.f90:611-615).
+//
+// The reference draws from one sequential generator (noise.f90:136-217,
+// idum = -1 at CTEMEBSD.f90:536) in pixel order, which no parallel
+// implementation can reproduce draw for draw.  Here every pixel of every
+// pattern has its own counter-based stream: Philox4x32-10 (Salmon, Moraes,
+// Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC 2011)
+// keyed by the seed, with the counter (pattern index, pixel index), so the
+// noise does not depend on launch shape, chunking or device.  The sampler
+// is inversion by sequential search for small means and Hormann's
+// transformed rejection with squeeze, PTRS ("The transformed rejection
+// method for generating Poisson random variables", Insurance: Mathematics
+// and Economics 12, 1993), for means >= 10.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ebsd {
+
+struct Philox4 {
+    uint32_t v[4];
+};
+
+__device__ __forceinline__ Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2,
+                                                 uint32_t c3, uint32_t k0, uint32_t k1)
+{
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;  // round multipliers
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;  // key schedule (Weyl)
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(M0, c0), lo0 = M0 * c0;
+        const uint32_t hi1 = __umulhi(M1, c2), lo1 = M1 * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += W0;
+        k1 += W1;
+    }
+    Philox4 out;
+    out.v[0] = c0;
+    out.v[1] = c1;
+    out.v[2] = c2;
+    out.v[3] = c3;
+    return out;
+}
+
+// Uniform in (0, 1): 24 random bits, centred in their interval.
+__device__ __forceinline__ float u01(uint32_t x)
+{
+    return ((float)(x >> 8) + 0.5f) * (1.0f / 16777216.0f);
+}
+
+// Per-pixel stream: four uniforms per Philox call; the call index is the
+// fourth counter word, so a rejection loop draws fresh blocks.  The block
+// is held in registers and read with selects (no local memory).
+struct PixelRng {
+    uint32_t c0, c1, c2, k0, k1, call;
+    Philox4 blk;
+    int used;
+    __device__ PixelRng(uint64_t seed, uint64_t pattern, uint32_t pixel)
+        : c0((uint32_t)pattern), c1((uint32_t)(pattern >> 32)), c2(pixel),
+          k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), call(0), used(4)
+    {
+    }
+    __device__ float next()
+    {
+        if (used == 4) {
+            blk = philox4x32_10(c0, c1, c2, call++, k0, k1);
+            used = 0;
+        }
+        const uint32_t x = used == 0 ? blk.v[0] : used == 1 ? blk.v[1] : used == 2 ? blk.v[2]
+                                                                                    : blk.v[3];
+        ++used;
+        return u01(x);
+    }
+};
+
+// One Poisson(lambda) draw.  lambda <= 0 (or NaN) gives 0.
+__device__ __forceinline__ float poisson_draw(float lambda, PixelRng& rng)
+{
+    if (!(lambda > 0.0f)) return 0.0f;
+    if (lambda < 10.0f) {
+        // inversion: walk the cumulative distribution from k = 0
+        const float u = rng.next();
+        float p = expf(-lambda), cdf = p;
+        int k = 0;
+        while (u > cdf && k < 200) {
+            ++k;
+            p *= lambda / (float)k;
+            cdf += p;
+        }
+        return (float)k;
+    }
+    // PTRS, Hormann (1993), constants from the paper
+    const float slam = sqrtf(lambda), loglam = logf(lambda);
+    const float b = 0.931f + 2.53f * slam;
+    const float a = -0.059f + 0.02483f * b;
+    const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
+    const float vr = 0.9277f - 3.6224f / (b - 2.0f);
+    for (int it = 0; it < 64; ++it) {  // acceptance > 0.85 per try
+        const float U = rng.next() - 0.5f;
+        const float V = rng.next();
+        const float us = 0.5f - fabsf(U);
+        const float k = floorf((2.0f * a / us + b) * U + lambda + 0.43f);
+        if (us >= 0.07f && V <= vr) return k;
+        if (k < 0.0f || (us < 0.013f && V > us)) continue;
+        if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <=
+            -lambda + k * loglam - lgammaf(k + 1.0f))
+            return k;
+    }
+    return floorf(lambda + 0.5f);  // not reached in practice (p < 1e-50)
+}
+
+}  // namespace ebsd

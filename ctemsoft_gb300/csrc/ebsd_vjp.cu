@@ -47,6 +47,84 @@ __device__ __forceinline__ void warp_reduce_scatter(float (&v)[KP], int lane)
     for (; off > 0; off >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
 }
 
+// Value and the six derivatives (w0, w1, w2, xpc, ypc, L) of output pixel p
+// of orientation o, before binning.
+template <int NV>
+__device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const VjpParams& vp,
+                                                     int p, int64_t o, uint64_t pol,
+                                                     float pref, float& val, float (&J)[6])
+{
+        const float4 q = __ldg(prm.quats + o);
+    const float4 r = ldg4_keep(prm.rg + p, pol);
+    float d0, d1, d2;
+    rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
+    const float nd = sqrtf(fmaf(d0, d0, fmaf(d1, d1, d2 * d2)));
+    const float h0 = d0 / nd, h1 = d1 / nd, h2 = d2 / nd;
+    float c0 = d0, c1 = d1, c2 = d2;
+    normalize_fold(c0, c1, c2);
+    const float s = h2 < 0.0f ? -1.0f : 1.0f;
+    float LX, LY, dX[3], dY[3];
+    lambert_inverse_jac(c0, c1, c2, prm.spi2, prm.accurate != 0, LX, LY, dX, dY);
+    float dx, dy;
+    int nix, niy;
+    const int ix0 = lambert_cell(prm.scl * LX, prm.npx, dx, nix);
+    const int iy0 = lambert_cell(prm.scl * LY, prm.npy, dy, niy);
+    const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
+    const float dxm = 1.0f - dx, dym = 1.0f - dy;
+    const float4* m00 = prm.master + ((int64_t)iy0 * prm.gx + ix0) * NV;
+    const float4* m10 = prm.master + ((int64_t)iy0 * prm.gx + ix1) * NV;
+    const float4* m01 = prm.master + ((int64_t)iy1 * prm.gx + ix0) * NV;
+    const float4* m11 = prm.master + ((int64_t)iy1 * prm.gx + ix1) * NV;
+    float P = 0.0f, gX = 0.0f, gY = 0.0f, gW0 = 0.0f, gW1 = 0.0f, gW2 = 0.0f;
+    // one float4 group of bins at a time: unrolling would hoist all
+    // 7*NV vector loads and spill
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c) {
+        const float4 A = ldg4_keep(m00 + c, pol), B = ldg4_keep(m10 + c, pol),
+                     C = ldg4_keep(m01 + c, pol), D = ldg4_keep(m11 + c, pol);
+        const float4 wc = ldg4_keep(prm.W + (int64_t)c * prm.P + p, pol);
+        const float4 e0 = ldg4_keep(vp.dW + (int64_t)(0 * NV + c) * prm.P + p, pol);
+        const float4 e1 = ldg4_keep(vp.dW + (int64_t)(1 * NV + c) * prm.P + p, pol);
+        const float4 e2 = ldg4_keep(vp.dW + (int64_t)(2 * NV + c) * prm.P + p, pol);
+#define EBSD_BIN(f)                                                                        \
+{                                                                                      \
+    const float bv = fmaf(A.f, dxm * dym, fmaf(B.f, dx * dym, fmaf(C.f, dxm * dy, D.f * dx * dy))); \
+    P = fmaf(wc.f, bv, P);                                                              \
+    gX = fmaf(wc.f, fmaf(B.f - A.f, dym, (D.f - C.f) * dy), gX);                         \
+    gY = fmaf(wc.f, fmaf(C.f - A.f, dxm, (D.f - B.f) * dx), gY);                         \
+    gW0 = fmaf(e0.f, bv, gW0);                                                          \
+    gW1 = fmaf(e1.f, bv, gW1);                                                          \
+    gW2 = fmaf(e2.f, bv, gW2);                                                          \
+}
+        EBSD_BIN(x) EBSD_BIN(y) EBSD_BIN(z) EBSD_BIN(w)
+#undef EBSD_BIN
+    }
+    val = pref * P;
+    const float sx = prm.scl * pref * gX, sy = prm.scl * pref * gY;
+    const float gc0 = sx * dX[0] + sy * dY[0];
+    const float gc1 = sx * dX[1] + sy * dY[1];
+    const float gc2 = sx * dX[2] + sy * dY[2];
+    const float pr = gc0 * h0 + gc1 * h1 + gc2 * h2;
+    const float k = s / nd;
+    const float g0 = k * (gc0 - pr * h0), g1 = k * (gc1 - pr * h1), g2 = k * (gc2 - pr * h2);
+    J[0] = d1 * g2 - d2 * g1;
+    J[1] = d2 * g0 - d0 * g2;
+    J[2] = d0 * g1 - d1 * g0;
+    // M^T g = conj(q) (x) (0,g) (x) q
+    const float u0 = -(g0 * q.y) - g1 * q.z - g2 * q.w;
+    const float u1 = g0 * q.x + g1 * q.w - g2 * q.z;
+    const float u2 = -(g0 * q.w) + g1 * q.x + g2 * q.y;
+    const float u3 = g0 * q.z - g1 * q.y + g2 * q.x;
+    const float m0 = q.x * u1 - q.y * u0 - q.z * u3 + q.w * u2;
+    const float m1 = q.x * u2 + q.y * u3 - q.z * u0 - q.w * u1;
+    const float m2 = q.x * u3 - q.y * u2 + q.z * u1 - q.w * u0;
+    const float4 r0 = ldg4_keep(vp.drg + p, pol), r1 = ldg4_keep(vp.drg + prm.P + p, pol),
+                 r2 = ldg4_keep(vp.drg + 2 * (int64_t)prm.P + p, pol);
+    J[3] = m0 * r0.x + m1 * r0.y + m2 * r0.z + pref * gW0;
+    J[4] = m0 * r1.x + m1 * r1.y + m2 * r1.z + pref * gW1;
+    J[5] = m0 * r2.x + m1 * r2.y + m2 * r2.z + pref * gW2;
+}
+
 template <int NV, int MODE>
 __global__ void __launch_bounds__(256, 3) k_vjp(const FwdParams prm, const VjpParams vp,
                                                  int tile_y, int tiles_x, int ntiles, int opc)
@@ -69,6 +147,7 @@ __global__ void __launch_bounds__(256, 3) k_vjp(const FwdParams prm, const VjpPa
     // per-pixel constants (direction, weights and their derivative tables)
     // are re-read per orientation; they are L1/L2 hits, and keeping them out
     // of registers lets 3 CTAs share an SM without spilling
+    const uint64_t pol = l2_policy_evict_last();
     const float pref = (float)prm.prefactor;
     const float ib2 = 1.0f / (float)(b * b);
     const int64_t rec = (int64_t)prm.out_nx * prm.out_ny;
@@ -77,77 +156,7 @@ __global__ void __launch_bounds__(256, 3) k_vjp(const FwdParams prm, const VjpPa
 
     for (int64_t o = o_begin; o < o_begin + opc && o < prm.n; ++o) {
         float val = 0.0f, J[6] = {0, 0, 0, 0, 0, 0};
-        if (inside) {
-            const float4 q = __ldg(prm.quats + o);
-            const float4 r = __ldg(prm.rg + p);
-            float d0, d1, d2;
-            rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
-            const float nd = sqrtf(fmaf(d0, d0, fmaf(d1, d1, d2 * d2)));
-            const float h0 = d0 / nd, h1 = d1 / nd, h2 = d2 / nd;
-            float c0 = d0, c1 = d1, c2 = d2;
-            normalize_fold(c0, c1, c2);
-            const float s = h2 < 0.0f ? -1.0f : 1.0f;
-            float LX, LY, dX[3], dY[3];
-            lambert_inverse_jac(c0, c1, c2, prm.spi2, prm.accurate != 0, LX, LY, dX, dY);
-            float dx, dy;
-            int nix, niy;
-            const int ix0 = lambert_cell(prm.scl * LX, prm.npx, dx, nix);
-            const int iy0 = lambert_cell(prm.scl * LY, prm.npy, dy, niy);
-            const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
-            const float dxm = 1.0f - dx, dym = 1.0f - dy;
-            const float4* m00 = prm.master + ((int64_t)iy0 * prm.gx + ix0) * NV;
-            const float4* m10 = prm.master + ((int64_t)iy0 * prm.gx + ix1) * NV;
-            const float4* m01 = prm.master + ((int64_t)iy1 * prm.gx + ix0) * NV;
-            const float4* m11 = prm.master + ((int64_t)iy1 * prm.gx + ix1) * NV;
-            float P = 0.0f, gX = 0.0f, gY = 0.0f, gW0 = 0.0f, gW1 = 0.0f, gW2 = 0.0f;
-            // one float4 group of bins at a time: unrolling would hoist all
-            // 7*NV vector loads and spill
-#pragma unroll 1
-            for (int c = 0; c < NV; ++c) {
-                const float4 A = __ldg(m00 + c), B = __ldg(m10 + c), C = __ldg(m01 + c),
-                             D = __ldg(m11 + c);
-                const float4 wc = __ldg(prm.W + (int64_t)c * prm.P + p);
-                const float4 e0 = __ldg(vp.dW + (int64_t)(0 * NV + c) * prm.P + p);
-                const float4 e1 = __ldg(vp.dW + (int64_t)(1 * NV + c) * prm.P + p);
-                const float4 e2 = __ldg(vp.dW + (int64_t)(2 * NV + c) * prm.P + p);
-#define EBSD_BIN(f)                                                                        \
-    {                                                                                      \
-        const float bv = fmaf(A.f, dxm * dym, fmaf(B.f, dx * dym, fmaf(C.f, dxm * dy, D.f * dx * dy))); \
-        P = fmaf(wc.f, bv, P);                                                              \
-        gX = fmaf(wc.f, fmaf(B.f - A.f, dym, (D.f - C.f) * dy), gX);                         \
-        gY = fmaf(wc.f, fmaf(C.f - A.f, dxm, (D.f - B.f) * dx), gY);                         \
-        gW0 = fmaf(e0.f, bv, gW0);                                                          \
-        gW1 = fmaf(e1.f, bv, gW1);                                                          \
-        gW2 = fmaf(e2.f, bv, gW2);                                                          \
-    }
-                EBSD_BIN(x) EBSD_BIN(y) EBSD_BIN(z) EBSD_BIN(w)
-#undef EBSD_BIN
-            }
-            val = pref * P;
-            const float sx = prm.scl * pref * gX, sy = prm.scl * pref * gY;
-            const float gc0 = sx * dX[0] + sy * dY[0];
-            const float gc1 = sx * dX[1] + sy * dY[1];
-            const float gc2 = sx * dX[2] + sy * dY[2];
-            const float pr = gc0 * h0 + gc1 * h1 + gc2 * h2;
-            const float k = s / nd;
-            const float g0 = k * (gc0 - pr * h0), g1 = k * (gc1 - pr * h1), g2 = k * (gc2 - pr * h2);
-            J[0] = d1 * g2 - d2 * g1;
-            J[1] = d2 * g0 - d0 * g2;
-            J[2] = d0 * g1 - d1 * g0;
-            // M^T g = conj(q) (x) (0,g) (x) q
-            const float u0 = -(g0 * q.y) - g1 * q.z - g2 * q.w;
-            const float u1 = g0 * q.x + g1 * q.w - g2 * q.z;
-            const float u2 = -(g0 * q.w) + g1 * q.x + g2 * q.y;
-            const float u3 = g0 * q.z - g1 * q.y + g2 * q.x;
-            const float m0 = q.x * u1 - q.y * u0 - q.z * u3 + q.w * u2;
-            const float m1 = q.x * u2 + q.y * u3 - q.z * u0 - q.w * u1;
-            const float m2 = q.x * u3 - q.y * u2 + q.z * u1 - q.w * u0;
-            const float4 r0 = __ldg(vp.drg + p), r1 = __ldg(vp.drg + prm.P + p),
-                         r2 = __ldg(vp.drg + 2 * (int64_t)prm.P + p);
-            J[3] = m0 * r0.x + m1 * r0.y + m2 * r0.z + pref * gW0;
-            J[4] = m0 * r1.x + m1 * r1.y + m2 * r1.z + pref * gW1;
-            J[5] = m0 * r2.x + m1 * r2.y + m2 * r2.z + pref * gW2;
-        }
+        if (inside) pixel_value_jacobian<NV>(prm, vp, p, o, pol, pref, val, J);
         // output-record value of this pixel's block
         float O = val;
         if (b > 1) {
@@ -238,6 +247,287 @@ __global__ void k_vjp_reduce(const float* __restrict__ partial, int64_t n, int n
     }
 }
 
+// ----------------------------------------------------------------------
+// Gauss-Newton on the normalised residual r = O/|O| - T/|T| (|r|^2/2 =
+// 1 - <O,T>/(|O||T|)).  With J_B = dO_B/dphi (6 parameters), a = sum O J/|O|:
+//   H = (sum_B J_B J_B^T - a a^T) / |O|^2,
+//   g = (a cos - sum_B T_B J_B / |T|) / |O|.
+// One pass per pattern accumulates sum J J^T (21), sum T J, sum O J and the
+// three dot products (36 numbers per CTA); J_B of a binned output pixel is
+// the block sum of the pixel Jacobians over b^2.
+constexpr int kGnK = 36;
+constexpr int kGnSys = 28;  // per pattern: H (21, packed upper), g (6), loss
+
+__device__ __forceinline__ int pk(int i, int j)  // packed index of H(i,j), i <= j
+{
+    return i * 6 - (i * (i - 1)) / 2 + (j - i);
+}
+
+template <int NV>
+__global__ void __launch_bounds__(256, 2) k_gn(const FwdParams prm, const VjpParams vp,
+                                               int tile_y, int tiles_x, int ntiles, int opc)
+{
+    extern __shared__ float sm[];  // val tile, 6 J tiles, [tile_y][36] warp sums
+    float* tile = sm;
+    float* jt = sm + 33 * tile_y;
+    float* red = jt + 6 * 33 * tile_y;
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int t = (int)(blockIdx.x % (unsigned)ntiles);
+    const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
+    const int x = (t % tiles_x) * kTileX + tx;
+    const int y = (t / tiles_x) * tile_y + ty;
+    const int b = vp.binning;
+    const bool inside = x < prm.numsx && y < prm.numsy && x < prm.out_nx * b &&
+                        y < prm.out_ny * b;
+    const int p = y * prm.numsx + x;
+    const uint64_t pol = l2_policy_evict_last();
+    const float pref = (float)prm.prefactor;
+    const float ib2 = 1.0f / (float)(b * b);
+    const int64_t rec = (int64_t)prm.out_nx * prm.out_ny;
+    const int X = x / b, Y = y / b;
+    const bool leader = (x % b == 0) && (y % b == 0);
+
+    for (int64_t o = o_begin; o < o_begin + opc && o < prm.n; ++o) {
+        float val = 0.0f, J[6] = {0, 0, 0, 0, 0, 0};
+        if (inside) pixel_value_jacobian<NV>(prm, vp, p, o, pol, pref, val, J);
+        float O = val, JB[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) JB[a] = J[a];
+        if (b > 1) {
+            tile[ty * 33 + tx] = val;
+#pragma unroll
+            for (int a = 0; a < 6; ++a) jt[(a * tile_y + ty) * 33 + tx] = inside ? J[a] : 0.0f;
+            __syncthreads();
+            if (inside) {
+                const int bx = tx - tx % b, by = ty - ty % b;
+                float s2 = 0.0f;
+                for (int jj = 0; jj < b; ++jj)
+                    for (int ii = 0; ii < b; ++ii) s2 += tile[(by + jj) * 33 + bx + ii];
+                O = s2 * ib2;
+                if (leader) {
+#pragma unroll
+                    for (int a = 0; a < 6; ++a) {
+                        float sj = 0.0f;
+                        for (int jj = 0; jj < b; ++jj)
+                            for (int ii = 0; ii < b; ++ii)
+                                sj += jt[(a * tile_y + ty + jj) * 33 + tx + ii];
+                        JB[a] = sj * ib2;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        float acc[16], accm[32];
+#pragma unroll
+        for (int a = 0; a < 16; ++a) acc[a] = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 32; ++a) accm[a] = 0.0f;
+        if (inside) {
+            const float dv = vp.data[o * rec + (int64_t)Y * prm.out_nx + X];
+            const float cT = dv * ib2, cO = O * ib2;
+#pragma unroll
+            for (int a = 0; a < 6; ++a) {
+                acc[a] = cT * J[a];
+                acc[6 + a] = cO * J[a];
+            }
+            if (leader) {
+                acc[12] = O * O;
+                acc[13] = O * dv;
+                acc[14] = dv * dv;
+#pragma unroll
+                for (int i = 0; i < 6; ++i)
+#pragma unroll
+                    for (int j = i; j < 6; ++j) accm[pk(i, j)] = JB[i] * JB[j];
+            }
+        }
+        warp_reduce_scatter<16>(acc, tx);
+        warp_reduce_scatter<32>(accm, tx);
+        if (tx % 2 == 0 && tx / 2 < 15) red[ty * kGnK + tx / 2] = acc[0];
+        if (tx < 21) red[ty * kGnK + 15 + tx] = accm[0];
+        __syncthreads();
+        if (tid < kGnK) {
+            float s2 = 0.0f;
+            for (int wy = 0; wy < tile_y; ++wy) s2 += red[wy * kGnK + tid];
+            vp.partial[(o * ntiles + t) * kGnK + tid] = s2;
+        }
+        __syncthreads();
+    }
+}
+
+// Per orientation: binary64 sums of the partials, then H, g and the loss.
+__global__ void k_gn_reduce(const float* __restrict__ partial, int64_t n, int ntiles,
+                            double* __restrict__ sys, float* __restrict__ loss)
+{
+    const int64_t o = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (o >= n) return;
+    double sacc[kGnK];
+#pragma unroll
+    for (int a = 0; a < kGnK; ++a) sacc[a] = 0.0;
+    for (int t = lane; t < ntiles; t += 32) {
+        const float* pp = partial + ((int64_t)o * ntiles + t) * kGnK;
+#pragma unroll
+        for (int a = 0; a < kGnK; ++a) sacc[a] += (double)pp[a];
+    }
+#pragma unroll
+    for (int a = 0; a < kGnK; ++a)
+        for (int off = 16; off > 0; off >>= 1) sacc[a] += __shfl_xor_sync(0xffffffffu, sacc[a], off);
+    if (lane != 0) return;
+    double* out = sys + o * kGnSys;
+    const double soo = sacc[12], sot = sacc[13], stt = sacc[14];
+    if (!(soo > 0.0) || !(stt > 0.0)) {
+        for (int a = 0; a < kGnSys; ++a) out[a] = 0.0;
+        if (loss) loss[o] = 0.0f;
+        return;
+    }
+    const double nO = sqrt(soo), nT = sqrt(stt), cosv = sot / (nO * nT);
+    double av[6];
+    for (int i = 0; i < 6; ++i) av[i] = sacc[6 + i] / nO;
+    for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 6; ++j)
+            out[pk(i, j)] = (sacc[15 + pk(i, j)] - av[i] * av[j]) / soo;
+    for (int i = 0; i < 6; ++i) out[21 + i] = (av[i] * cosv - sacc[i] / nT) / nO;
+    out[27] = 1.0 - cosv;
+    if (loss) loss[o] = (float)(1.0 - cosv);
+}
+
+__device__ __forceinline__ double hget(const double* sys, int i, int j)
+{
+    return i <= j ? sys[pk(i, j)] : sys[pk(j, i)];
+}
+
+// inverse of a symmetric 3x3 (row-major); false if not positive definite
+__device__ __forceinline__ bool inv3(const double A[9], double Ai[9])
+{
+    const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8],
+                 c02 = A[3] * A[7] - A[4] * A[6];
+    const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
+    if (!(det > 0.0) || !isfinite(det)) return false;
+    const double id = 1.0 / det;
+    Ai[0] = c00 * id;
+    Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
+    Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
+    Ai[3] = c01 * id;
+    Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
+    Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
+    Ai[6] = c02 * id;
+    Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
+    Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+    return true;
+}
+
+// damped rotation block A = H_rr + lambda diag(H_rr)
+__device__ __forceinline__ void rot_block(const double* sys, double lambda, double A[9])
+{
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) A[i * 3 + j] = hget(sys, i, j);
+    for (int i = 0; i < 3; ++i) A[i * 4] *= 1.0 + lambda;
+}
+
+// Pattern-centre Schur complement: sum over patterns of
+//   S_n = C_n - B_n^T A_n^-1 B_n,  r_n = -(g_p - B_n^T A_n^-1 g_r),
+// in binary64, one partial per block (fixed order), 12 numbers each.
+__global__ void k_gn_schur(const double* __restrict__ sys, int64_t n, double lambda,
+                           double* __restrict__ partial)
+{
+    __shared__ double sh[256][12];
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double v[12];
+    for (int a = 0; a < 12; ++a) v[a] = 0.0;
+    if (o < n) {
+        const double* sp = sys + o * kGnSys;
+        double A[9], Ai[9];
+        rot_block(sp, lambda, A);
+        if (inv3(A, Ai)) {
+            double B[3][3], AiB[3][3], Aig[3];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) B[i][j] = hget(sp, i, 3 + j);
+            for (int i = 0; i < 3; ++i) {
+                Aig[i] = 0.0;
+                for (int k = 0; k < 3; ++k) Aig[i] += Ai[i * 3 + k] * sp[21 + k];
+                for (int j = 0; j < 3; ++j) {
+                    AiB[i][j] = 0.0;
+                    for (int k = 0; k < 3; ++k) AiB[i][j] += Ai[i * 3 + k] * B[k][j];
+                }
+            }
+            for (int i = 0; i < 3; ++i) {
+                for (int j = 0; j < 3; ++j) {
+                    double bab = 0.0;
+                    for (int k = 0; k < 3; ++k) bab += B[k][i] * AiB[k][j];
+                    v[i * 3 + j] = hget(sp, 3 + i, 3 + j) - bab;
+                }
+                double bag = 0.0;
+                for (int k = 0; k < 3; ++k) bag += B[k][i] * Aig[k];
+                v[9 + i] = -(sp[24 + i] - bag);
+            }
+        }
+    }
+    for (int a = 0; a < 12; ++a) sh[threadIdx.x][a] = v[a];
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+            for (int a = 0; a < 12; ++a) sh[threadIdx.x][a] += sh[threadIdx.x + w][a];
+        __syncthreads();
+    }
+    if (threadIdx.x < 12) partial[(int64_t)blockIdx.x * 12 + threadIdx.x] = sh[0][threadIdx.x];
+}
+
+__global__ void k_gn_schur_final(const double* __restrict__ partial, int nblocks,
+                                 double* __restrict__ out)
+{
+    if (threadIdx.x >= 12) return;
+    double s2 = 0.0;
+    for (int bk = 0; bk < nblocks; ++bk) s2 += partial[(int64_t)bk * 12 + threadIdx.x];
+    out[threadIdx.x] = s2;
+}
+
+// Per pattern: d_rot = -A^-1 (g_r + B dpc), q <- exp(d_rot) (x) q, renormalised.
+__global__ void k_gn_update(const double* __restrict__ sys, int64_t n, double lambda,
+                            const double* __restrict__ dpc, float4* __restrict__ quats,
+                            float* __restrict__ step)
+{
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const double* sp = sys + o * kGnSys;
+    double A[9], Ai[9], rhs[3];
+    rot_block(sp, lambda, A);
+    for (int i = 0; i < 3; ++i) {
+        rhs[i] = sp[21 + i];
+        if (dpc)
+            for (int j = 0; j < 3; ++j) rhs[i] += hget(sp, i, 3 + j) * dpc[j];
+    }
+    double w[3] = {0.0, 0.0, 0.0};
+    if (inv3(A, Ai))
+        for (int i = 0; i < 3; ++i)
+            w[i] = -(Ai[i * 3] * rhs[0] + Ai[i * 3 + 1] * rhs[1] + Ai[i * 3 + 2] * rhs[2]);
+    const double th = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    step[o] = (float)th;
+    if (!(th > 0.0) || !isfinite(th)) return;
+    const double c = cos(0.5 * th), sn = sin(0.5 * th) / th;
+    const double e0 = c, e1 = sn * w[0], e2 = sn * w[1], e3 = sn * w[2];
+    const float4 q = quats[o];
+    double r0 = e0 * q.x - e1 * q.y - e2 * q.z - e3 * q.w;
+    double r1 = e0 * q.y + e1 * q.x + e2 * q.w - e3 * q.z;
+    double r2 = e0 * q.z - e1 * q.w + e2 * q.x + e3 * q.y;
+    double r3 = e0 * q.w + e1 * q.z - e2 * q.y + e3 * q.x;
+    const double nq = sqrt(r0 * r0 + r1 * r1 + r2 * r2 + r3 * r3);
+    quats[o] = make_float4((float)(r0 / nq), (float)(r1 / nq), (float)(r2 / nq), (float)(r3 / nq));
+}
+
+template <int NV>
+cudaError_t launch_gn_nv(const FwdParams& p, const VjpParams& vp, int tile_y, cudaStream_t s)
+{
+    const int tiles_x = (p.numsx + kTileX - 1) / kTileX;
+    const int tiles_y = (p.numsy + tile_y - 1) / tile_y;
+    const int ntiles = tiles_x * tiles_y;
+    const int opc = vp.opc;
+    const int64_t blocks = ((p.n + opc - 1) / opc) * ntiles;
+    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+    const size_t smem = sizeof(float) * (33 * tile_y * 7 + kGnK * tile_y);
+    k_gn<NV><<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, vp, tile_y, tiles_x, ntiles, opc);
+    return cudaGetLastError();
+}
+
 template <int NV>
 cudaError_t launch_vjp_nv(const FwdParams& p, const VjpParams& vp, int mode, int tile_y,
                           cudaStream_t s)
@@ -292,6 +582,49 @@ cudaError_t launch_vjp(const FwdParams& p, const VjpParams& vp, int NV, int mode
     else
         k_vjp_reduce<EBSD_VJP_COTANGENT><<<rb, 32 * wpb, 0, s>>>(vp.partial, p.n, ntiles, vp.loss,
                                                                  vp.grad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gn_accumulate(const FwdParams& p, const VjpParams& vp, int NV, int tile_y,
+                                 double* sys, float* loss, cudaStream_t s)
+{
+    if (p.n <= 0) return cudaSuccess;
+    cudaError_t e;
+    switch (NV) {
+        case 1: e = launch_gn_nv<1>(p, vp, tile_y, s); break;
+        case 2: e = launch_gn_nv<2>(p, vp, tile_y, s); break;
+        case 3: e = launch_gn_nv<3>(p, vp, tile_y, s); break;
+        case 4: e = launch_gn_nv<4>(p, vp, tile_y, s); break;
+        case 5: e = launch_gn_nv<5>(p, vp, tile_y, s); break;
+        case 6: e = launch_gn_nv<6>(p, vp, tile_y, s); break;
+        case 7: e = launch_gn_nv<7>(p, vp, tile_y, s); break;
+        case 8: e = launch_gn_nv<8>(p, vp, tile_y, s); break;
+        default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    const int ntiles = vjp_tiles(p, tile_y);
+    const int wpb = 4;
+    k_gn_reduce<<<(unsigned)((p.n + wpb - 1) / wpb), 32 * wpb, 0, s>>>(vp.partial, p.n, ntiles,
+                                                                      sys, loss);
+    return cudaGetLastError();
+}
+
+int gn_schur_blocks(int64_t n) { return (int)((n + 255) / 256); }
+
+cudaError_t launch_gn_schur(const double* sys, int64_t n, double lambda, double* partial,
+                            double* out, cudaStream_t s)
+{
+    const int nb = gn_schur_blocks(n);
+    if (nb > 0) k_gn_schur<<<nb, 256, 0, s>>>(sys, n, lambda, partial);
+    k_gn_schur_final<<<1, 32, 0, s>>>(partial, nb, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gn_update(const double* sys, int64_t n, double lambda, const double* dpc,
+                             float4* quats, float* step, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    k_gn_update<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(sys, n, lambda, dpc, quats, step);
     return cudaGetLastError();
 }
 

@@ -214,6 +214,45 @@ int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue*
 int ebsd_vjp_noalloc(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
                      int32_t mode, const float* data, float* loss, float* grad);
 
+/* Gauss-Newton refinement of orientations and, optionally, the detector's
+ * shared pattern centre against target records (no reference counterpart).
+ * The residual is the normalised-pattern difference O/|O| - T/|T|, so
+ * |r|^2/2 is the loss 1 - <O,T>/(|O||T|) of ebsd_vjp.  quats, targets and
+ * loss are device memory; quats are updated in place (q <- exp(dw) (x) q,
+ * renormalised).  Epilogue as ebsd_vjp (binning allowed; no gamma/noise).
+ *
+ * Two phases per step, so callers spread over several GPUs can sum the
+ * pattern-centre system across ranks in between:
+ *   ebsd_gn_accumulate: per-pattern normal equations (kept in the handle)
+ *     and, if pc_system != NULL, the pattern centre's Schur-complement
+ *     system S dpc = r, 12 doubles (S row-major, then r), over this call's
+ *     patterns; loss (may be NULL) receives each pattern's loss.
+ *   ebsd_gn_apply: with dpc = NULL (orientations only) or the solved centre
+ *     step, updates every orientation of the last accumulate; *max_step gets
+ *     the largest rotation step in radians.
+ * damping is Levenberg-Marquardt lambda relative to the diagonal. */
+int ebsd_gn_accumulate(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
+                       const float* targets, double damping, double* pc_system, float* loss);
+int ebsd_gn_apply(ebsd_handle* h, float* quats, int64_t n, double damping, const double* dpc,
+                  double* max_step);
+
+typedef struct {
+    int32_t max_iterations; /* Gauss-Newton steps at most */
+    int32_t refine_pc;      /* 1: also refine (xpc, ypc, L) of the shared detector */
+    double damping;         /* Levenberg-Marquardt lambda, relative to the diagonal */
+    double tol_rad;         /* stop when every rotation step is below this (rad) */
+    double tol_pc;          /* ... and the pattern-centre step below this (px, um) */
+} ebsd_gn_options;
+
+/* The whole refinement on one GPU: ebsd_gn_accumulate / solve / apply until
+ * the steps fall below the tolerances; after each centre step the detector
+ * tables are rebuilt for the new geometry (the prefactor is kept: the loss
+ * does not depend on it).  *geom (in/out) receives the refined detector;
+ * *iterations the number of steps taken. */
+int ebsd_refine(ebsd_handle* h, float* quats, int64_t n, const ebsd_epilogue* e,
+                const float* targets, const ebsd_gn_options* opt, float* loss,
+                ebsd_geometry* geom, int32_t* iterations);
+
 /* Lambert cells of the loop (CTEMEBSD.f90:584-598) for n quaternions:
  * nix/niy (grid indices in -npx..npx) and the scaled Lambert coordinates
  * ixy0/ixy1, each [n][numsy][numsx].  Host or device pointers.  For parity
