@@ -489,10 +489,8 @@ def _perturb(q, sigma_deg, rng):
 
 
 def _misorientation_deg(a, b):
-    import numpy as np
-    d = np.abs((a.astype(np.float64) * b.astype(np.float64)).sum(axis=1))
-    d /= np.linalg.norm(a, axis=1) * np.linalg.norm(b, axis=1)
-    return np.degrees(2 * np.arccos(np.clip(d, -1, 1)))
+    from ctemsoft_gb300 import synth
+    return synth.misorientation_deg(a, b)
 
 
 def _fd_gauss_newton(h, q, epi, targets, geom, acc, iters, damping, chunk=10000):

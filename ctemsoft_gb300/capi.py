@@ -80,7 +80,8 @@ class Namelist(C.Structure):
                 ("beamcurrent", C.c_double), ("dwelltime", C.c_double),
                 ("energymin", C.c_float), ("energymax", C.c_float), ("binning", C.c_int32),
                 ("gammavalue", C.c_float), ("scalingmode", C.c_char * 4),
-                ("axisangle", C.c_float * 4), ("poisson", C.c_int32), ("seed", C.c_int64)]
+                ("axisangle", C.c_float * 4), ("poisson", C.c_int32), ("seed", C.c_int64),
+                ("resume", C.c_int32)]
 
 
 _P = C.c_void_p

@@ -4,6 +4,7 @@
 #include "ebsd_host.h"
 
 #include <cctype>
+#include <unistd.h>
 #include <cerrno>
 #include <cmath>
 #include <cstdlib>
@@ -158,6 +159,18 @@ bool FortranReader::skip()
 }
 
 FortranWriter::FortranWriter(const char* path) { f_ = path ? fopen(path, "wb") : nullptr; }
+
+FortranWriter::FortranWriter(const char* path, long long keep_bytes)
+{
+    f_ = path ? fopen(path, "r+b") : nullptr;
+    if (!f_) return;
+    // drop a partial trailing record, then append after the kept bytes
+    if (fflush(f_) != 0 || ftruncate(fileno(f_), (off_t)keep_bytes) != 0 ||
+        fseeko(f_, (off_t)keep_bytes, SEEK_SET) != 0) {
+        fclose(f_);
+        f_ = nullptr;
+    }
+}
 
 FortranWriter::~FortranWriter() { close(); }
 
@@ -368,6 +381,7 @@ int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
     nml->binning = 1;
     nml->poisson = 1;
     nml->seed = 1;
+    nml->resume = 0;
 
     std::ifstream in(path ? path : "");
     if (!in) {
@@ -475,6 +489,8 @@ int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
             }
         } else if (key == "poisson") {
             ok = v.size() == 1 && parse_logical(v[0], &nml->poisson);
+        } else if (key == "resume") {
+            ok = v.size() == 1 && parse_logical(v[0], &nml->resume);
         } else if (key == "seed") {
             int64_t x;
             ok = v.size() == 1 && parse_int(v[0], &x);

@@ -55,6 +55,8 @@ private:
 class FortranWriter {
 public:
     explicit FortranWriter(const char* path);
+    // Re-open an existing file, truncate it to keep_bytes and append there.
+    FortranWriter(const char* path, long long keep_bytes);
     ~FortranWriter();
     bool ok() const { return f_ != nullptr; }
     bool write(const void* data, size_t bytes);

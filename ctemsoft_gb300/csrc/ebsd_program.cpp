@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -149,17 +150,52 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
     if (rc) return herr(rc);
 
     // output header (:555-561): binned dimensions whenever binning != 1
-    host::FortranWriter out(nml.datafile);
-    if (!out.ok()) return fail(EBSD_EIO, std::string("cannot create output file '") + nml.datafile + "'");
     int32_t hdr[3] = {nml.numsx, nml.numsy, (int32_t)numeuler};
     if (nml.binning != 1) {
         hdr[0] = nml.numsx / nml.binning;
         hdr[1] = nml.numsy / nml.binning;
     }
-    if (!out.write(hdr, sizeof hdr)) return fail(EBSD_EIO, "output header write failed");
+    const size_t rec = (size_t)rx * ry;
+    // resume: an output file with the same header keeps its complete
+    // records (20-byte header record, then 4*rec + 8 bytes per pattern)
+    int64_t done = 0;
+    if (nml.resume) {
+        FILE* f = fopen(nml.datafile, "rb");
+        if (f) {
+            int32_t head[5] = {0, 0, 0, 0, 0};
+            const bool hok = fread(head, 4, 5, f) == 5 && head[0] == 12 && head[4] == 12 &&
+                             head[1] == hdr[0] && head[2] == hdr[1] && head[3] == hdr[2];
+            fseeko(f, 0, SEEK_END);
+            const long long size = (long long)ftello(f);
+            fclose(f);
+            if (hok) {
+                const long long per = 4LL * (long long)rec + 8;
+                done = std::min<int64_t>(numeuler, (size - 20) / per);
+                while (done > 0) {  // the last counted record must be complete
+                    FILE* g2 = fopen(nml.datafile, "rb");
+                    int32_t m1 = 0, m2 = 0;
+                    const long long off = 20 + (done - 1) * per;
+                    bool ok2 = g2 && fseeko(g2, off, SEEK_SET) == 0 && fread(&m1, 4, 1, g2) == 1 &&
+                               fseeko(g2, off + 4 + 4LL * (long long)rec, SEEK_SET) == 0 &&
+                               fread(&m2, 4, 1, g2) == 1;
+                    if (g2) fclose(g2);
+                    if (ok2 && m1 == (int32_t)(4 * rec) && m2 == m1) break;
+                    --done;
+                }
+                say(" resuming after %lld complete patterns\n", (long long)done);
+            }
+        }
+    }
+    std::unique_ptr<host::FortranWriter> outp;
+    if (done > 0)
+        outp.reset(new host::FortranWriter(nml.datafile, 20 + done * (4LL * (long long)rec + 8)));
+    else
+        outp.reset(new host::FortranWriter(nml.datafile));
+    host::FortranWriter& out = *outp;
+    if (!out.ok()) return fail(EBSD_EIO, std::string("cannot create output file '") + nml.datafile + "'");
+    if (done == 0 && !out.write(hdr, sizeof hdr)) return fail(EBSD_EIO, "output header write failed");
 
     const auto t0 = std::chrono::steady_clock::now();                 // Time_start (:567)
-    const size_t rec = (size_t)rx * ry;
     const int64_t chunk = std::max<int64_t>(
         1, std::min<int64_t>(numeuler, (int64_t)((size_t(256) << 20) / (rec * sizeof(float)))));
     PinnedGuard pg;
@@ -169,7 +205,7 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
     }
     std::thread writer;
     bool write_ok = true;
-    for (int64_t o0 = 0, c = 0; o0 < numeuler; o0 += chunk, ++c) {
+    for (int64_t o0 = done, c = 0; o0 < numeuler; o0 += chunk, ++c) {
         const int64_t m = std::min(chunk, numeuler - o0);
         float* buf = pg.p[c & 1];
         rc = ebsd_forward(h, quats.data() + 4 * o0, m, &epi, buf);

@@ -165,6 +165,21 @@ def shoemake_quaternions(n: int, seed: int) -> np.ndarray:
     return q.astype(np.float32)
 
 
+def misorientation_deg(a, b) -> np.ndarray:
+    """Rotation angle (degrees, no crystal symmetry) between quaternion rows
+    of a and b: 2 atan2(|vec(conj(a) b)|, |scalar(conj(a) b)|) in binary64,
+    which keeps its accuracy near zero where arccos of the dot product
+    cannot resolve angles below about 0.03 degrees from float32 inputs."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    a = a / np.linalg.norm(a, axis=1, keepdims=True)
+    b = b / np.linalg.norm(b, axis=1, keepdims=True)
+    s0 = (a * b).sum(axis=1)
+    v = (a[:, :1] * b[:, 1:] - b[:, :1] * a[:, 1:]
+         - np.cross(a[:, 1:], b[:, 1:]))
+    return np.degrees(2 * np.arctan2(np.linalg.norm(v, axis=1), np.abs(s0)))
+
+
 def _cached(key, make):
     """Large arrays are generated once per machine and kept as .npy files in
     $EBSD_SYNTH_CACHE (default: <tmp>/ctemsoft_gb300_synth)."""

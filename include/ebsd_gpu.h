@@ -317,6 +317,8 @@ typedef struct {
     /* keys this library adds; defaults keep the reference's behaviour */
     int32_t poisson; /* default 1: noise on, as the reference always is */
     int64_t seed;    /* default 1 */
+    int32_t resume;  /* default 0; 1: keep the complete records of an existing
+                        output file with the same header and compute the rest */
 } ebsd_namelist;
 
 /* Parse a namelist file (Fortran &EBSDdata ... / group). */
