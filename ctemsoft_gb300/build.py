@@ -33,7 +33,7 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
              f"-I{CUDA_HOME / 'include'}"]
 
-CU_SOURCES = ["ebsd_setup.cu", "ebsd_forward.cu", "ebsd_vjp.cu", "ebsd_capi.cu"]
+CU_SOURCES = ["ebsd_setup.cu", "ebsd_forward.cu", "ebsd_vjp.cu", "ebsd_so3.cu", "ebsd_capi.cu"]
 CXX_SOURCES = ["ebsd_host.cpp", "ebsd_program.cpp"]
 HEADERS = ["ebsd_internal.h", "ebsd_device.cuh", "ebsd_host.h", "ebsd_noise.cuh"]
 
@@ -89,8 +89,8 @@ def build_library(verbose: bool = False) -> Path:
 def build_oracle() -> Path:
     """Compile the CPU oracle (test infrastructure) ``oracle/liboracle.so``."""
     out = ORACLE / "liboracle.so"
-    srcs = [ORACLE / "ebsd_oracle.c", ORACLE / "ebsd_oracle_grad.c"]
-    if _newer(srcs[0], [srcs[1], ORACLE / "ebsd_oracle.h"], out):
+    srcs = [ORACLE / "ebsd_oracle.c", ORACLE / "ebsd_oracle_grad.c", ORACLE / "ebsd_oracle_so3.c"]
+    if _newer(srcs[0], [*srcs[1:], ORACLE / "ebsd_oracle.h"], out):
         cc = os.environ.get("CC", "gcc")
         _run([cc, "-O3", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-std=c11",
               "-shared", "-o", str(out), *map(str, srcs), "-lm"])

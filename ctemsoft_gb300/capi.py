@@ -116,6 +116,8 @@ _SIGS = {
     "ebsd_vjp_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), C.c_int32, _P, _P,
                                    _P]),
     "ebsd_get_detector": (C.c_int, [_P, _P, _P, _P, _P]),
+    "ebsd_sample_rfz": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P, C.c_int64,
+                                  C.POINTER(C.c_int64)]),
     "ebsd_run_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "ebsd_read_mc_file": (C.c_int, [C.c_char_p, C.POINTER(MCHeader), _P]),
     "ebsd_read_master_file": (C.c_int, [C.c_char_p, C.POINTER(MasterHeader), _P, _P, _P]),
@@ -354,6 +356,20 @@ class Handle:
         _check(lib().ebsd_get_detector(self._h, _ptr(W), _ptr(rgx), _ptr(rgy), _ptr(rgz)),
                self._h)
         return W, rgx, rgy, rgz
+
+    def sample_rfz(self, nsteps: int, pgnum: int):
+        """Cubochoric sampling of the Rodrigues fundamental zone of point
+        group pgnum (SampleRFZ).  Returns (rods (n, 3) float64, quats (n, 4)
+        float32), in the reference's grid order."""
+        cnt = C.c_int64()
+        _check(lib().ebsd_sample_rfz(self._h, nsteps, pgnum, None, None, 0, C.byref(cnt)),
+               self._h)
+        n = cnt.value
+        r = np.empty((n, 3), np.float64)
+        q = np.empty((n, 4), np.float32)
+        _check(lib().ebsd_sample_rfz(self._h, nsteps, pgnum, _ptr(r), _ptr(q), n,
+                                     C.byref(cnt)), self._h)
+        return r, q
 
 
 def run_namelist(path: str, device: int = 0, quiet: bool = True) -> None:

@@ -97,6 +97,10 @@ struct ebsd_handle {
     std::vector<int> batch_key;
     cudaStream_t batch_stream = nullptr;
     std::map<int, int> batch_grid;  // NV -> persistent grid size
+
+    // fundamental-zone sampler: codes, chunk scan, device copies of outputs
+    DeviceBuf rfz;
+    DeviceBuf rfz_out;
 };
 
 namespace {
@@ -161,6 +165,17 @@ PtrKind ptr_kind(const void* p)
         case cudaMemoryTypeHost: return kPinned;
         default: return kPageable;
     }
+}
+
+// Caller device memory that the kernels read or write as float4 (the
+// quaternions) must be 16-byte aligned, doubles 8-byte aligned: a
+// misaligned vector access would fault, so such pointers are refused.
+int check_aligned(ebsd_handle* h, const void* p, size_t a, const char* what)
+{
+    if (((uintptr_t)p & (a - 1)) != 0)
+        return set_err(h, EBSD_EINVAL, "%s: device pointer %p is not %zu-byte aligned", what, p,
+                       a);
+    return EBSD_OK;
 }
 
 int activate(ebsd_handle* h)
@@ -332,6 +347,8 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
     cudaFree(h->gn_sys.ptr);
     cudaFree(h->gn_aux.ptr);
     cudaFree(h->batch_table.ptr);
+    cudaFree(h->rfz.ptr);
+    cudaFree(h->rfz_out.ptr);
     if (h->batch_table_host) cudaFreeHost(h->batch_table_host);
     if (h->batch_exec) cudaGraphExecDestroy(h->batch_exec);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -644,6 +661,9 @@ extern "C" int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const
     if (qk != kDevice) {
         rc = check_quats_host(h, quats, n);
         if (rc) return rc;
+    } else {
+        rc = check_aligned(h, quats, 16, "ebsd_forward quats");
+        if (rc) return rc;
     }
     cudaStream_t s = h->stream;
 
@@ -777,6 +797,9 @@ extern "C" int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebs
     if (!qdev) {
         rc = check_quats_host(h, quats, n);
         if (rc) return rc;
+    } else {
+        rc = check_aligned(h, quats, 16, "ebsd_vjp quats");
+        if (rc) return rc;
     }
     // chunk so that partials and staged records stay bounded
     const size_t budget = size_t(256) << 20;
@@ -900,6 +923,8 @@ extern "C" int ebsd_vjp_noalloc(ebsd_handle* h, const float* quats, int64_t n,
         (loss && ptr_kind(loss) != kDevice))
         return set_err(h, EBSD_EINVAL,
                        "ebsd_vjp_noalloc: quats, data, loss and grad must be device memory");
+    rc = check_aligned(h, quats, 16, "ebsd_vjp_noalloc quats");
+    if (rc) return rc;
     rc = activate(h);
     if (rc) return rc;
     float* scratch = nullptr;
@@ -957,7 +982,7 @@ int gn_check(ebsd_handle* h, const ebsd_epilogue* e, const float* quats, const f
     if (h->NV > 8) return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: at most 32 energy bins");
     if (ptr_kind(quats) != kDevice || ptr_kind(targets) != kDevice)
         return set_err(h, EBSD_EINVAL, "Gauss-Newton: quats and targets must be device memory");
-    return EBSD_OK;
+    return check_aligned(h, quats, 16, "Gauss-Newton quats");
 }
 
 }  // namespace
@@ -1035,6 +1060,8 @@ extern "C" int ebsd_gn_apply(ebsd_handle* h, float* quats, int64_t n, double dam
                        "had %lld", (long long)n, (long long)h->gn_n);
     if (!quats || ptr_kind(quats) != kDevice)
         return set_err(h, EBSD_EINVAL, "ebsd_gn_apply: quats must be device memory");
+    rc = check_aligned(h, quats, 16, "ebsd_gn_apply quats");
+    if (rc) return rc;
     rc = activate(h);
     if (rc) return rc;
     cudaStream_t s = h->stream;
@@ -1130,6 +1157,7 @@ namespace {
 struct BatchGroup {
     int NV;
     bool noise;
+    int ty;  // tile height of the group's launch
     std::vector<BatchJob> jobs;
 };
 
@@ -1157,6 +1185,8 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         if (!J.quats || !J.out) return set_err(h, EBSD_EINVAL, "job %d: null pointer", j);
         if (ptr_kind(J.quats) != kDevice || ptr_kind(J.out) != kDevice)
             return set_err(h, EBSD_EINVAL, "job %d: quats and out must be device memory", j);
+        if (((uintptr_t)J.quats & 15) != 0)
+            return set_err(h, EBSD_EINVAL, "job %d: quats not 16-byte aligned", j);
         if (src->NV > 8)
             return set_err(h, EBSD_EUNSUPPORTED, "job %d: more than 32 energy bins", j);
         BatchJob b;
@@ -1166,23 +1196,27 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         b.p.quats = (const float4*)J.quats;
         b.p.out = J.out;
         b.p.n = J.n;
+        const int ty = batch_tile_y(b.p.mode == EBSD_SCALING_NOT ? 1 : b.p.binning);
         b.tiles_x = (b.p.numsx + kTileX - 1) / kTileX;
-        b.ntiles = b.tiles_x * ((b.p.numsy + kBatchTileY - 1) / kBatchTileY);
-        b.opc = std::max(4, src->cfg.orient_per_cta);  // items of >= 4 orientations
+        b.ntiles = b.tiles_x * ((b.p.numsy + ty - 1) / ty);
+        // items of 32 x ty pixels x opc orientations, >= 1024 pixel-patterns
+        b.opc = std::max(32 / ty, src->cfg.orient_per_cta);
         b.items = (long long)b.ntiles * ((J.n + b.opc - 1) / b.opc);
         const bool noise = J.epilogue.poisson != 0;
         auto g = std::find_if(groups.begin(), groups.end(), [&](const BatchGroup& x) {
-            return x.NV == src->NV && x.noise == noise;
+            return x.NV == src->NV && x.noise == noise && x.ty == ty;
         });
         if (g == groups.end()) {
-            groups.push_back({src->NV, noise, {}});
+            groups.push_back({src->NV, noise, ty, {}});
             g = groups.end() - 1;
         }
         g->jobs.push_back(b);
     }
     if (groups.empty()) return EBSD_OK;
     std::sort(groups.begin(), groups.end(), [](const BatchGroup& a, const BatchGroup& b) {
-        return a.NV != b.NV ? a.NV < b.NV : a.noise < b.noise;
+        if (a.NV != b.NV) return a.NV < b.NV;
+        if (a.noise != b.noise) return a.noise < b.noise;
+        return a.ty < b.ty;
     });
 
     // table: [headers][counters][jobs of group 0][jobs of group 1]...
@@ -1198,7 +1232,7 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
     CK(h, cudaStreamSynchronize(h->stream), "batch");
     std::vector<int> key;
     for (auto& g : groups) {
-        key.push_back(g.NV * 2 + (g.noise ? 1 : 0));
+        key.push_back(g.NV * 32 + (g.noise ? 16 : 0) + g.ty);
         key.push_back((int)g.jobs.size());
     }
     const bool use_graph = (flags & EBSD_BATCH_GRAPH) != 0;
@@ -1239,10 +1273,10 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         memcpy(ht + gi * sizeof(BatchHeader), &hd, sizeof hd);
         memcpy(ht + job_off + jo * sizeof(BatchJob), g.jobs.data(), g.jobs.size() * sizeof(BatchJob));
         jo += g.jobs.size();
-        const int gk = g.NV * 2 + (g.noise ? 1 : 0);
+        const int gk = g.NV * 32 + (g.noise ? 16 : 0) + g.ty;
         auto it = h->batch_grid.find(gk);
         if (it == h->batch_grid.end())
-            it = h->batch_grid.emplace(gk, batched_grid(g.NV, g.noise)).first;
+            it = h->batch_grid.emplace(gk, batched_grid(g.NV, g.noise, g.ty)).first;
         grids[gi] = it->second;
     }
     cudaStream_t s = h->stream;
@@ -1256,7 +1290,7 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
                 (const BatchJob*)(dt + job_off + j0 * sizeof(BatchJob)),
                 (const BatchHeader*)(dt + gi * sizeof(BatchHeader)),
                 (unsigned long long*)(dt + cnt_off) + gi, groups[gi].NV, groups[gi].noise,
-                grids[gi], s);
+                groups[gi].ty, grids[gi], s);
             j0 += groups[gi].jobs.size();
         }
         return e;
@@ -1446,7 +1480,10 @@ extern "C" int ebsd_cells(ebsd_handle* h, const float* quats, int64_t n, int32_t
     cudaStream_t s = h->stream;
     DeviceBuf qb, ob;
     const float4* dq = (const float4*)quats;
-    if (ptr_kind(quats) != kDevice) {
+    if (ptr_kind(quats) == kDevice) {
+        rc = check_aligned(h, quats, 16, "ebsd_cells quats");
+        if (rc) return rc;
+    } else {
         rc = ensure(h, qb, sizeof(float4) * n, "quaternions");
         if (rc) return rc;
         CK(h, cudaMemcpyAsync(qb.ptr, quats, sizeof(float4) * n, cudaMemcpyHostToDevice, s), "upload");
@@ -1528,3 +1565,92 @@ int handle_set_error(ebsd_handle* h, int code, const char* msg)
 int global_set_error(int code, const char* msg) { return set_err(nullptr, code, "%s", msg); }
 }  // namespace host
 }  // namespace ebsd
+
+// ----------------------------------------------------------------------
+// Orientation lists for dictionaries: cubochoric sampling of a Rodrigues
+// fundamental zone (so3.f90:267-371)
+
+namespace {
+
+// so3.f90:73-74: FZ type and principal-axis order per point group 1..32
+const int kFZtype[32] = {0, 0, 1, 1, 1, 2, 2, 2, 1, 1, 1, 2, 2, 2, 2, 1,
+                         1, 2, 2, 2, 1, 1, 1, 2, 2, 2, 2, 3, 3, 4, 3, 4};
+const int kFZorder[32] = {0, 0, 2, 2, 2, 2, 2, 2, 4, 4, 4, 4, 4, 4, 4, 3,
+                          3, 3, 3, 3, 6, 6, 6, 6, 6, 6, 6, 0, 0, 0, 0, 0};
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" int ebsd_sample_rfz(ebsd_handle* h, int32_t nsteps, int32_t pgnum, double* rods,
+                               float* quats, int64_t capacity, int64_t* count)
+{
+    if (!h) return set_err(nullptr, EBSD_EINVAL, "null handle");
+    if (!count) return set_err(h, EBSD_EINVAL, "ebsd_sample_rfz: count is null");
+    if (nsteps < 1 || nsteps > kMaxRfzSteps)
+        return set_err(h, EBSD_EINVAL, "ebsd_sample_rfz: nsteps %d outside 1..%d", nsteps,
+                       kMaxRfzSteps);
+    if (pgnum < 1 || pgnum > 32)
+        return set_err(h, EBSD_EINVAL, "ebsd_sample_rfz: point group %d outside 1..32", pgnum);
+    if (capacity < 0) return set_err(h, EBSD_EINVAL, "ebsd_sample_rfz: negative capacity");
+    int rc = activate(h);
+    if (rc) return rc;
+    const So3Consts K = so3_constants();
+    // the grid coordinates exactly as the reference accumulates them
+    std::vector<double> xs;
+    const double delta = K.semi / (double)nsteps;
+    for (double x = -K.semi; x < K.semi; x = x + delta) xs.push_back(x);
+    const int m = (int)xs.size();
+    const long long total = (long long)m * m * m;
+    const long long nchunks = rfz_chunks(total);
+    const size_t o_xs = 0, o_code = align256(sizeof(double) * m);
+    const size_t o_chunk = o_code + align256((size_t)total);
+    const size_t o_enter = o_chunk + align256(rfz_chunk_bytes() * (size_t)nchunks);
+    const size_t o_off = o_enter + align256(sizeof(int) * (size_t)nchunks);
+    const size_t o_cnt = o_off + align256(sizeof(long long) * (size_t)nchunks);
+    rc = ensure(h, h->rfz, o_cnt + 256, "fundamental-zone sampling");
+    if (rc) return rc;
+    char* base = (char*)h->rfz.ptr;
+    cudaStream_t s = h->stream;
+    const bool want = capacity > 0 && (rods || quats);
+    const bool rdev = rods && ptr_kind(rods) == kDevice;
+    const bool qdev = quats && ptr_kind(quats) == kDevice;
+    if (rdev) {
+        rc = check_aligned(h, rods, 8, "ebsd_sample_rfz rods");
+        if (rc) return rc;
+    }
+    if (qdev) {
+        rc = check_aligned(h, quats, 16, "ebsd_sample_rfz quats");
+        if (rc) return rc;
+    }
+    double* d_rods = rdev ? rods : nullptr;
+    float* d_quats = qdev ? quats : nullptr;
+    if (want && ((rods && !rdev) || (quats && !qdev))) {
+        const size_t rb = rods && !rdev ? align256(sizeof(double) * 3 * (size_t)capacity) : 0;
+        const size_t qb = quats && !qdev ? sizeof(float) * 4 * (size_t)capacity : 0;
+        rc = ensure(h, h->rfz_out, rb + qb, "fundamental-zone sampling output");
+        if (rc) return rc;
+        if (rods && !rdev) d_rods = (double*)h->rfz_out.ptr;
+        if (quats && !qdev) d_quats = (float*)((char*)h->rfz_out.ptr + rb);
+    }
+    CK(h, cudaMemcpyAsync(base + o_xs, xs.data(), sizeof(double) * m, cudaMemcpyHostToDevice, s),
+       "grid upload");
+    CK(h, launch_rfz(K, (const double*)(base + o_xs), m, kFZtype[pgnum - 1], kFZorder[pgnum - 1],
+                     (uint8_t*)(base + o_code), base + o_chunk, (int*)(base + o_enter),
+                     (long long*)(base + o_off), (long long*)(base + o_cnt),
+                     want ? capacity : 0, want ? d_rods : nullptr, want ? d_quats : nullptr,
+                     !want, s),
+       "fundamental-zone sampling");
+    long long n = 0;
+    CK(h, cudaMemcpyAsync(&n, base + o_cnt, sizeof n, cudaMemcpyDeviceToHost, s), "count copy");
+    CK(h, cudaStreamSynchronize(s), "fundamental-zone sampling");
+    const long long w = want ? std::min<long long>(n, capacity) : 0;
+    if (w > 0 && rods && !rdev)
+        CK(h, cudaMemcpy(rods, d_rods, sizeof(double) * 3 * (size_t)w, cudaMemcpyDeviceToHost),
+           "rods copy");
+    if (w > 0 && quats && !qdev)
+        CK(h, cudaMemcpy(quats, d_quats, sizeof(float) * 4 * (size_t)w, cudaMemcpyDeviceToHost),
+           "quaternion copy");
+    *count = n;
+    return EBSD_OK;
+}

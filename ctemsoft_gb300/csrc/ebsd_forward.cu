@@ -168,51 +168,58 @@ __global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y
 // detectors, binnings and masters.  Each CTA takes the next item with one
 // atomic increment and stops when the queue is exhausted -- no CTA waits
 // on another, so nothing can spin.  Jobs are ordered by item_begin.
-template <int NV, bool NOISE>
-__global__ void __launch_bounds__(256) k_forward_batched(const BatchJob* __restrict__ jobs,
-                                                         const BatchHeader* __restrict__ hdr,
-                                                         unsigned long long* __restrict__ counter)
+// TY is the tile height (CTA = 32 x TY threads); a group's jobs all use it.
+// Both heights get 1024 resident threads per SM at up to 64 registers.
+template <int NV, bool NOISE, int TY>
+__global__ void __launch_bounds__(32 * TY, 32 / TY) k_forward_batched(const BatchJob* __restrict__ jobs,
+                                                             const BatchHeader* __restrict__ hdr,
+                                                             unsigned long long* __restrict__ counter)
 {
-    __shared__ float tile[kBatchTileY * 33];
+    __shared__ float tile[TY * 33];
     __shared__ long long s_begin[kBatchMaxJobsSmem];  // item_begin of each job
-    __shared__ long long s_item[2];
-    __shared__ int s_job[2];
+    __shared__ long long s_obegin[2];
+    __shared__ int s_job[2], s_tile[2];
     const int njobs = hdr->njobs;
     const long long total = hdr->total_items;
     const bool cached = njobs <= kBatchMaxJobsSmem;
     if (cached)
         for (int j = threadIdx.x; j < njobs; j += blockDim.x) s_begin[j] = jobs[j].item_begin;
     __syncthreads();
-    // thread 0 claims items one ahead: while the CTA computes item k, the
-    // claim and job lookup of item k+1 are already in flight
+    // Thread 0 claims and decodes items one ahead: while the CTA computes
+    // item k, the claim, the job search and the (64-bit) tile/orientation
+    // split of item k+1 are already done by one thread instead of all.
     auto claim = [&](int slot) {
         const long long it = (long long)atomicAdd(counter, 1ULL);
-        s_item[slot] = it;
-        if (it < total) {
-            int lo = 0, hi = njobs - 1;  // last job with item_begin <= it
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                const long long b = cached ? s_begin[mid] : jobs[mid].item_begin;
-                if (b <= it)
-                    lo = mid;
-                else
-                    hi = mid - 1;
-            }
-            s_job[slot] = lo;
+        if (it >= total) {
+            s_job[slot] = -1;
+            return;
         }
+        int lo = 0, hi = njobs - 1;  // last job with item_begin <= it
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            const long long b = cached ? s_begin[mid] : jobs[mid].item_begin;
+            if (b <= it)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const BatchJob& J = jobs[lo];
+        const long long local = it - J.item_begin;
+        const long long ob = local / J.ntiles;
+        s_job[slot] = lo;
+        s_tile[slot] = (int)(local - ob * J.ntiles);
+        s_obegin[slot] = ob * J.opc;
     };
     if (threadIdx.x == 0) claim(0);
     __syncthreads();
     for (int slot = 0;; slot ^= 1) {
-        const long long it = s_item[slot];
-        if (it >= total) break;
         const int job = s_job[slot];
+        if (job < 0) break;
+        const int t = s_tile[slot];
+        const int64_t o_begin = s_obegin[slot];
         if (threadIdx.x == 0) claim(slot ^ 1);
         const BatchJob& J = jobs[job];
-        const long long local = it - J.item_begin;
-        const int t = (int)(local % J.ntiles);
-        const int64_t o_begin = (int64_t)(local / J.ntiles) * J.opc;
-        forward_tile<NV, false, NOISE>(J.p, kBatchTileY, J.tiles_x, t, o_begin, J.opc, tile);
+        forward_tile<NV, false, NOISE>(J.p, TY, J.tiles_x, t, o_begin, J.opc, tile);
         __syncthreads();
     }
 }
@@ -266,62 +273,75 @@ cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
                       : launch_nv2<NV, false, false>(p, cfg, s);
 }
 
-template <int NV>
-cudaError_t launch_batched_nv(const BatchJob* jobs, const BatchHeader* hdr,
-                              unsigned long long* counter, int grid, bool noise, cudaStream_t s)
+template <int NV, bool NOISE, int TY>
+cudaError_t launch_batched3(const BatchJob* jobs, const BatchHeader* hdr,
+                            unsigned long long* counter, int grid, cudaStream_t s)
 {
-    if (noise)
-        k_forward_batched<NV, true><<<grid, 32 * kBatchTileY, 0, s>>>(jobs, hdr, counter);
-    else
-        k_forward_batched<NV, false><<<grid, 32 * kBatchTileY, 0, s>>>(jobs, hdr, counter);
+    k_forward_batched<NV, NOISE, TY><<<grid, 32 * TY, 0, s>>>(jobs, hdr, counter);
     return cudaGetLastError();
 }
 
 template <int NV>
-int batched_grid_nv(bool noise)
+cudaError_t launch_batched_nv(const BatchJob* jobs, const BatchHeader* hdr,
+                              unsigned long long* counter, int grid, bool noise, int ty,
+                              cudaStream_t s)
+{
+    if (ty == 4)
+        return noise ? launch_batched3<NV, true, 4>(jobs, hdr, counter, grid, s)
+                     : launch_batched3<NV, false, 4>(jobs, hdr, counter, grid, s);
+    return noise ? launch_batched3<NV, true, 8>(jobs, hdr, counter, grid, s)
+                 : launch_batched3<NV, false, 8>(jobs, hdr, counter, grid, s);
+}
+
+template <int NV, bool NOISE, int TY>
+int batched_grid3()
 {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (noise)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV, true>,
-                                                      32 * kBatchTileY, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV, false>,
-                                                      32 * kBatchTileY, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV, NOISE, TY>, 32 * TY,
+                                                  0);
     return sms * (per > 0 ? per : 1);
+}
+
+template <int NV>
+int batched_grid_nv(bool noise, int ty)
+{
+    if (ty == 4) return noise ? batched_grid3<NV, true, 4>() : batched_grid3<NV, false, 4>();
+    return noise ? batched_grid3<NV, true, 8>() : batched_grid3<NV, false, 8>();
 }
 
 }  // namespace
 
 cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
-                                   unsigned long long* counter, int NV, bool noise, int grid,
-                                   cudaStream_t s)
+                                   unsigned long long* counter, int NV, bool noise, int ty,
+                                   int grid, cudaStream_t s)
 {
+    if (ty != 4 && ty != 8) return cudaErrorInvalidValue;
     switch (NV) {
-        case 1: return launch_batched_nv<1>(jobs, hdr, counter, grid, noise, s);
-        case 2: return launch_batched_nv<2>(jobs, hdr, counter, grid, noise, s);
-        case 3: return launch_batched_nv<3>(jobs, hdr, counter, grid, noise, s);
-        case 4: return launch_batched_nv<4>(jobs, hdr, counter, grid, noise, s);
-        case 5: return launch_batched_nv<5>(jobs, hdr, counter, grid, noise, s);
-        case 6: return launch_batched_nv<6>(jobs, hdr, counter, grid, noise, s);
-        case 7: return launch_batched_nv<7>(jobs, hdr, counter, grid, noise, s);
-        case 8: return launch_batched_nv<8>(jobs, hdr, counter, grid, noise, s);
+        case 1: return launch_batched_nv<1>(jobs, hdr, counter, grid, noise, ty, s);
+        case 2: return launch_batched_nv<2>(jobs, hdr, counter, grid, noise, ty, s);
+        case 3: return launch_batched_nv<3>(jobs, hdr, counter, grid, noise, ty, s);
+        case 4: return launch_batched_nv<4>(jobs, hdr, counter, grid, noise, ty, s);
+        case 5: return launch_batched_nv<5>(jobs, hdr, counter, grid, noise, ty, s);
+        case 6: return launch_batched_nv<6>(jobs, hdr, counter, grid, noise, ty, s);
+        case 7: return launch_batched_nv<7>(jobs, hdr, counter, grid, noise, ty, s);
+        case 8: return launch_batched_nv<8>(jobs, hdr, counter, grid, noise, ty, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
-int batched_grid(int NV, bool noise)
+int batched_grid(int NV, bool noise, int ty)
 {
     switch (NV) {
-        case 1: return batched_grid_nv<1>(noise);
-        case 2: return batched_grid_nv<2>(noise);
-        case 3: return batched_grid_nv<3>(noise);
-        case 4: return batched_grid_nv<4>(noise);
-        case 5: return batched_grid_nv<5>(noise);
-        case 6: return batched_grid_nv<6>(noise);
-        case 7: return batched_grid_nv<7>(noise);
-        case 8: return batched_grid_nv<8>(noise);
+        case 1: return batched_grid_nv<1>(noise, ty);
+        case 2: return batched_grid_nv<2>(noise, ty);
+        case 3: return batched_grid_nv<3>(noise, ty);
+        case 4: return batched_grid_nv<4>(noise, ty);
+        case 5: return batched_grid_nv<5>(noise, ty);
+        case 6: return batched_grid_nv<6>(noise, ty);
+        case 7: return batched_grid_nv<7>(noise, ty);
+        case 8: return batched_grid_nv<8>(noise, ty);
         default: return 0;
     }
 }

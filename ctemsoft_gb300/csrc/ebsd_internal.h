@@ -62,7 +62,8 @@ struct VjpParams {
 };
 
 // Batched pattern loop (ebsd_forward.cu): a table of jobs in device memory.
-constexpr int kBatchTileY = 8;  // CTA = 32 x 8 pixels; binning up to 8
+// batched CTAs are 32 x 4 pixels for binning up to 4, 32 x 8 for binning 8
+inline int batch_tile_y(int binning) { return binning > 4 ? 8 : 4; }
 constexpr int kBatchMaxJobsSmem = 512;  // job starts cached in shared memory
 
 struct BatchJob {
@@ -139,8 +140,26 @@ cudaError_t launch_gn_update(const double* sys, int64_t n, double lambda, const 
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s);
 cudaError_t launch_cells(const FwdParams& p, int NV, cudaStream_t s);
 cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
-                                   unsigned long long* counter, int NV, bool noise, int grid,
-                                   cudaStream_t s);
-int batched_grid(int NV, bool noise);
+                                   unsigned long long* counter, int NV, bool noise, int ty,
+                                   int grid, cudaStream_t s);
+int batched_grid(int NV, bool noise, int ty);
+
+// Cubochoric fundamental-zone sampling (ebsd_so3.cu).  Constants of
+// Lambert.f90:246-280 in binary64.
+struct So3Consts {
+    double Pi, sPi, srt, pref, semi, sc, R1, r2, r22, pi12, pi8, prek, r24, rvmax2, edge;
+    double BP[6];
+};
+So3Consts so3_constants();
+constexpr int kMaxRfzSteps = 1000;  // (2N+1)^3 codes: 8 GB at the limit
+long long rfz_chunks(long long total);
+size_t rfz_chunk_bytes();
+// code: m^3 bytes; chunk: rfz_chunks * rfz_chunk_bytes; enter/offset: one
+// per chunk; count: one value.  rods (3 doubles) / quats (float4) may be
+// null; at most cap entries are written.
+cudaError_t launch_rfz(const So3Consts& K, const double* xs, int m, int type, int order,
+                       uint8_t* code, void* chunk, int* enter, long long* offset,
+                       long long* count, long long cap, double* rods, float* quats,
+                       bool count_only, cudaStream_t s);
 
 }  // namespace ebsd

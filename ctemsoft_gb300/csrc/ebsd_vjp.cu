@@ -54,7 +54,7 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
                                                      int p, int64_t o, uint64_t pol,
                                                      float pref, float& val, float (&J)[6])
 {
-        const float4 q = __ldg(prm.quats + o);
+    const float4 q = __ldg(prm.quats + o);
     const float4 r = ldg4_keep(prm.rg + p, pol);
     float d0, d1, d2;
     rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
@@ -75,9 +75,13 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     const float4* m10 = prm.master + ((int64_t)iy0 * prm.gx + ix1) * NV;
     const float4* m01 = prm.master + ((int64_t)iy1 * prm.gx + ix0) * NV;
     const float4* m11 = prm.master + ((int64_t)iy1 * prm.gx + ix1) * NV;
-    float P = 0.0f, gX = 0.0f, gY = 0.0f, gW0 = 0.0f, gW1 = 0.0f, gW2 = 0.0f;
+    // Weighted corner sums SA = sum_k W_k A_k etc. give P and both bilinear
+    // slopes with four FMAs per bin; the weight derivatives need the
+    // per-bin bilinear value bv.
+    const float w00 = dxm * dym, w10 = dx * dym, w01 = dxm * dy, w11 = dx * dy;
+    float SA = 0.0f, SB = 0.0f, SC = 0.0f, SD = 0.0f, gW0 = 0.0f, gW1 = 0.0f, gW2 = 0.0f;
     // one float4 group of bins at a time: unrolling would hoist all
-    // 7*NV vector loads and spill
+    // 8*NV vector loads and spill
 #pragma unroll 1
     for (int c = 0; c < NV; ++c) {
         const float4 A = ldg4_keep(m00 + c, pol), B = ldg4_keep(m10 + c, pol),
@@ -88,10 +92,11 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
         const float4 e2 = ldg4_keep(vp.dW + (int64_t)(2 * NV + c) * prm.P + p, pol);
 #define EBSD_BIN(f)                                                                        \
 {                                                                                      \
-    const float bv = fmaf(A.f, dxm * dym, fmaf(B.f, dx * dym, fmaf(C.f, dxm * dy, D.f * dx * dy))); \
-    P = fmaf(wc.f, bv, P);                                                              \
-    gX = fmaf(wc.f, fmaf(B.f - A.f, dym, (D.f - C.f) * dy), gX);                         \
-    gY = fmaf(wc.f, fmaf(C.f - A.f, dxm, (D.f - B.f) * dx), gY);                         \
+    const float bv = fmaf(A.f, w00, fmaf(B.f, w10, fmaf(C.f, w01, D.f * w11)));         \
+    SA = fmaf(wc.f, A.f, SA);                                                           \
+    SB = fmaf(wc.f, B.f, SB);                                                           \
+    SC = fmaf(wc.f, C.f, SC);                                                           \
+    SD = fmaf(wc.f, D.f, SD);                                                           \
     gW0 = fmaf(e0.f, bv, gW0);                                                          \
     gW1 = fmaf(e1.f, bv, gW1);                                                          \
     gW2 = fmaf(e2.f, bv, gW2);                                                          \
@@ -99,6 +104,9 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
         EBSD_BIN(x) EBSD_BIN(y) EBSD_BIN(z) EBSD_BIN(w)
 #undef EBSD_BIN
     }
+    const float P = fmaf(SA, w00, fmaf(SB, w10, fmaf(SC, w01, SD * w11)));
+    const float gX = fmaf(SB - SA, dym, (SD - SC) * dy);
+    const float gY = fmaf(SC - SA, dxm, (SD - SB) * dx);
     val = pref * P;
     const float sx = prm.scl * pref * gX, sy = prm.scl * pref * gY;
     const float gc0 = sx * dX[0] + sy * dY[0];
@@ -125,9 +133,15 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     J[5] = m0 * r2.x + m1 * r2.y + m2 * r2.z + pref * gW2;
 }
 
+// Resident CTAs per SM the register allocation is held to (256 threads
+// each); a build-time tuning knob.
+#ifndef EBSD_VJP_MIN_BLOCKS
+#define EBSD_VJP_MIN_BLOCKS 3
+#endif
+
 template <int NV, int MODE>
-__global__ void __launch_bounds__(256, 3) k_vjp(const FwdParams prm, const VjpParams vp,
-                                                 int tile_y, int tiles_x, int ntiles, int opc)
+__global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
+    k_vjp(const FwdParams prm, const VjpParams vp, int tile_y, int tiles_x, int ntiles, int opc)
 {
     constexpr int K = MODE == EBSD_VJP_NDP ? 15 : 6;
     constexpr int KP = MODE == EBSD_VJP_NDP ? 16 : 8;

@@ -266,6 +266,31 @@ int ebsd_cells(ebsd_handle* h, const float* quats, int64_t n, int32_t* nix, int3
 int ebsd_get_detector(ebsd_handle* h, float* W, float* rgx, float* rgy, float* rgz);
 
 /* ------------------------------------------------------------------ */
+/* Dictionary orientation lists                                         */
+/* ------------------------------------------------------------------ */
+
+/* Cubochoric sampling of a Rodrigues fundamental zone: replaces SampleRFZ
+ * (so3.f90:267-371), which fills the linked list FZlist/FZcnt.  The grid
+ * has semi-edge pi^(2/3)/2 and step semi-edge/nsteps, walked x-outer,
+ * z-inner from -semi-edge while below +semi-edge, the coordinate
+ * accumulated by repeated addition in binary64 as the reference does;
+ * each point goes cube -> ball -> Rodrigues vector in binary64 and is kept
+ * if it lies in the fundamental zone of crystallographic point group pgnum
+ * (1..32, International Tables order, so3.f90:59-74).  Point groups of FZ
+ * type 0/1 keep the previous point's verdict for rotations of 179.999
+ * degrees and more, as the reference's loop does.
+ *   *count        number of members (always written);
+ *   rods          count x 3 doubles, the Rodrigues vectors, or NULL;
+ *   quats         count x 4 floats, the quaternions (scalar first) that
+ *                 the reference's ro2qu gives (via ax2om/om2qu), ready for
+ *                 ebsd_forward, or NULL.
+ * At most `capacity` entries are written, in grid order; call with
+ * capacity 0 to size the buffers.  Pointers are host or device memory.
+ * Needs no master or detector.  nsteps 1..1000. */
+int ebsd_sample_rfz(ebsd_handle* h, int32_t nsteps, int32_t pgnum, double* rods, float* quats,
+                    int64_t capacity, int64_t* count);
+
+/* ------------------------------------------------------------------ */
 /* File formats and the drop-in program                                 */
 /* ------------------------------------------------------------------ */
 

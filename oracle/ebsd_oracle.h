@@ -80,6 +80,18 @@ void oracle_epilogue_f64(const double* pat, int numsx, int numsy, int binning, i
                          double gammavalue, double* out);
 int oracle_max_threads(void);
 
+/* Cubochoric sampling of Rodrigues fundamental zones (ebsd_oracle_so3.c). */
+void oracle_so3_constants(double out[8]);
+int oracle_cu2ho_d(const double c[3], double res[3]);
+int oracle_ho2cu_d(const double h[3], double res[3]);
+void oracle_ho2ro_d(const double h[3], double res[3]);
+void oracle_cu2ro_d(const double c[3], double rod[3]);
+void oracle_ro2qu_d(const double r[3], double q[4]);
+int oracle_fz_type(int pgnum, int* order);
+int oracle_fz_code(const double rod[3], int type, int order);
+int64_t oracle_rfz_axis(int nsteps, double* xs, int64_t cap);
+int64_t oracle_sample_rfz(int nsteps, int pgnum, double* rods, int64_t cap);
+
 #ifdef __cplusplus
 }
 #endif

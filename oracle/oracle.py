@@ -68,15 +68,25 @@ _SIGS = {
     "oracle_epilogue_f32": (None, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, _P]),
     "oracle_epilogue_f64": (None, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _P]),
     "oracle_max_threads": (C.c_int, []),
+    "oracle_so3_constants": (None, [_P]),
+    "oracle_cu2ho_d": (C.c_int, [_P, _P]),
+    "oracle_ho2cu_d": (C.c_int, [_P, _P]),
+    "oracle_ho2ro_d": (None, [_P, _P]),
+    "oracle_cu2ro_d": (None, [_P, _P]),
+    "oracle_ro2qu_d": (None, [_P, _P]),
+    "oracle_fz_type": (C.c_int, [C.c_int, C.POINTER(C.c_int)]),
+    "oracle_fz_code": (C.c_int, [_P, C.c_int, C.c_int]),
+    "oracle_rfz_axis": (C.c_int64, [C.c_int, _P, C.c_int64]),
+    "oracle_sample_rfz": (C.c_int64, [C.c_int, C.c_int, _P, C.c_int64]),
 }
 
 _lib = None
 
 
 def build() -> Path:
-    src = HERE / "ebsd_oracle.c"
-    if not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime,
-                                                      (HERE / "ebsd_oracle.h").stat().st_mtime):
+    srcs = [HERE / n for n in ("ebsd_oracle.c", "ebsd_oracle_grad.c", "ebsd_oracle_so3.c",
+                               "ebsd_oracle.h")]
+    if not LIB.exists() or LIB.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
         subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
     return LIB
 
@@ -304,3 +314,75 @@ def max_threads() -> int:
 
 def host_threads() -> int:
     return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
+# ---------------------------------------------------------------------------
+# Cubochoric sampling of Rodrigues fundamental zones (ebsd_oracle_so3.c)
+
+def so3_constants():
+    """(cube semi-edge, sc, R1, prek, pref, rvmax2, pi8, srt) in binary64."""
+    out = np.zeros(8)
+    lib().oracle_so3_constants(_p(out))
+    return out
+
+
+def _map3(fn, xs):
+    x = np.ascontiguousarray(np.atleast_2d(xs), np.float64)
+    out = np.zeros_like(x)
+    f = getattr(lib(), fn)
+    for i in range(len(x)):
+        f(_p(x[i]), _p(out[i]))
+    return out
+
+
+def cu2ho(c):
+    return _map3("oracle_cu2ho_d", c)
+
+
+def ho2cu(h):
+    return _map3("oracle_ho2cu_d", h)
+
+
+def ho2ro(h):
+    return _map3("oracle_ho2ro_d", h)
+
+
+def cu2ro(c):
+    return _map3("oracle_cu2ro_d", c)
+
+
+def ro2qu(r):
+    x = np.ascontiguousarray(np.atleast_2d(r), np.float64)
+    out = np.zeros((len(x), 4))
+    for i in range(len(x)):
+        lib().oracle_ro2qu_d(_p(x[i]), _p(out[i]))
+    return out
+
+
+def fz_type(pgnum):
+    o = C.c_int()
+    t = lib().oracle_fz_type(pgnum, C.byref(o))
+    return t, o.value
+
+
+def fz_code(rod, pgnum):
+    t, o = fz_type(pgnum)
+    r = np.ascontiguousarray(rod, np.float64)
+    return lib().oracle_fz_code(_p(r), t, o)
+
+
+def rfz_axis(nsteps):
+    m = lib().oracle_rfz_axis(nsteps, None, 0)
+    xs = np.zeros(m)
+    lib().oracle_rfz_axis(nsteps, _p(xs), m)
+    return xs
+
+
+def sample_rfz(nsteps, pgnum):
+    """Rodrigues vectors (count, 3) of SampleRFZ(nsteps, pgnum), loop order."""
+    n = lib().oracle_sample_rfz(nsteps, pgnum, None, 0)
+    if n < 0:
+        raise ValueError("bad point group or step count")
+    rods = np.zeros((max(n, 1), 3))
+    lib().oracle_sample_rfz(nsteps, pgnum, _p(rods), n)
+    return rods[:n]

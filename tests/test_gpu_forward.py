@@ -279,3 +279,31 @@ def test_c2_subset_and_properties(built):
     assert np.array_equal(out, h.forward(-q, epi))
     assert np.array_equal(out, h.forward(q, epi))
     h.close()
+
+
+def test_misaligned_device_quaternions_are_refused(built):
+    """Kernels read quaternions as float4: a device pointer off a 16-byte
+    boundary is refused before any launch (forward, adjoint, cells)."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    wl = synth.tiny()
+    h, det, sr, num_el = _setup(wl)
+    epi = capi.epilogue(capi.prefactor(15.0, 100.0, num_el))
+    buf = torch.zeros(4 * 3 + 1, device="cuda")
+    bad = buf.data_ptr() + 4
+    out = torch.zeros((3, wl.numsy, wl.numsx), device="cuda")
+    L = capi.lib()
+    assert L.ebsd_forward(h.raw, bad, 3, C.byref(epi), capi._ptr(out)) == capi.EBSD_EINVAL
+    assert "aligned" in L.ebsd_last_error(h.raw).decode()
+    grad = torch.zeros((3, 6), device="cuda")
+    assert L.ebsd_vjp(h.raw, bad, 3, C.byref(epi), 0, capi._ptr(out), None,
+                      capi._ptr(grad)) == capi.EBSD_EINVAL
+    nix = torch.zeros((3, wl.numsy, wl.numsx), dtype=torch.int32, device="cuda")
+    fl = torch.zeros((3, wl.numsy, wl.numsx), device="cuda")
+    assert L.ebsd_cells(h.raw, bad, 3, capi._ptr(nix), capi._ptr(nix), capi._ptr(fl),
+                        capi._ptr(fl)) == capi.EBSD_EINVAL
+    # the aligned start of the same buffer works
+    good = buf[:12].view(3, 4)
+    good[:, 0] = 1.0
+    assert L.ebsd_forward(h.raw, good.data_ptr(), 3, C.byref(epi), capi._ptr(out)) == 0
+    h.close()
