@@ -81,7 +81,7 @@ class Namelist(C.Structure):
                 ("energymin", C.c_float), ("energymax", C.c_float), ("binning", C.c_int32),
                 ("gammavalue", C.c_float), ("scalingmode", C.c_char * 4),
                 ("axisangle", C.c_float * 4), ("poisson", C.c_int32), ("seed", C.c_int64),
-                ("resume", C.c_int32)]
+                ("resume", C.c_int32), ("ncubochoric", C.c_int32), ("pgnum", C.c_int32)]
 
 
 _P = C.c_void_p

@@ -86,6 +86,8 @@ struct ebsd_handle {
     int max_persist = 0, max_window = 0;
 
     LaunchCfg cfg;
+    int vjp_tile_y = 8;  // adjoint CTA height (binning must divide it)
+    int vjp_opc = 2;     // adjoint orientations per CTA
     int weights_fp64 = 1;
     int lambert_accurate = 0;
 
@@ -397,6 +399,14 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
         if (value < 1 || value > 64)
             return set_err(h, EBSD_EINVAL, "orient_per_cta must be in 1..64");
         h->cfg.orient_per_cta = (int)value;
+    } else if (k == "vjp_tile_y") {
+        if (value != 4 && value != 8)
+            return set_err(h, EBSD_EINVAL, "vjp_tile_y must be 4 or 8");
+        h->vjp_tile_y = (int)value;
+    } else if (k == "vjp_orient_per_cta") {
+        if (value < 1 || value > 64)
+            return set_err(h, EBSD_EINVAL, "vjp_orient_per_cta must be in 1..64");
+        h->vjp_opc = (int)value;
     } else {
         return set_err(h, EBSD_EINVAL, "unknown option '%s'", key);
     }
@@ -783,8 +793,8 @@ extern "C" int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebs
     vp.drg = h->d_drg;
     vp.dW = h->d_dW;
     vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
-    vp.opc = 2;
-    const int tile_y = 8;
+    vp.opc = h->vjp_opc;
+    const int tile_y = vp.binning > h->vjp_tile_y ? 8 : h->vjp_tile_y;
     if (vp.binning > tile_y)
         return set_err(h, EBSD_EUNSUPPORTED, "ebsd_vjp: binning %d exceeds the tile", vp.binning);
     const int K = mode == EBSD_VJP_NDP ? 15 : 6;

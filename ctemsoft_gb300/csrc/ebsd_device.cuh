@@ -127,13 +127,18 @@ __device__ __forceinline__ void lambert_inverse_jac(float x, float y, float z, f
     X = xb ? along : across;
     Y = xb ? across : along;
     if (!(rxy > 0.0f)) return;
-    const float rho = sqrtf(2.0f * rxy / (1.0f + z));
+    // The derivatives need relative accuracy, not the reference's rounding:
+    // the hardware reciprocal square root and fast divide (CUDA intrinsics,
+    // 2-ulp bounds) replace IEEE divisions here.
+    const float t = __fdividef(2.0f * rxy, 1.0f + z);
+    const float irho = rsqrtf(t);
+    const float rho = t * irho;
     const float sg = copysignf(1.0f, u);
-    const float irho = 1.0f / rho;
-    const float f = sg * rho / (spi2 * rxy);
+    const float ispi2 = __fdividef(1.0f, spi2);
+    const float f = sg * __fdividef(rho * ispi2, rxy);
     // d(along)/dz, d(across)/d(u, v, z)
     const float dal_z = -sg * spi2 * irho;
-    const float dac_u = -f * v, dac_v = f * u, dac_z = -sg * a * irho / spi2;
+    const float dac_u = -f * v, dac_v = f * u, dac_z = -sg * a * irho * ispi2;
     if (xb) {  // along = X (u = x), across = Y (v = y)
         dX[2] = dal_z;
         dY[0] = dac_u;

@@ -382,6 +382,8 @@ int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
     nml->poisson = 1;
     nml->seed = 1;
     nml->resume = 0;
+    nml->ncubochoric = 0;
+    nml->pgnum = 32;
 
     std::ifstream in(path ? path : "");
     if (!in) {
@@ -491,6 +493,10 @@ int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
             ok = v.size() == 1 && parse_logical(v[0], &nml->poisson);
         } else if (key == "resume") {
             ok = v.size() == 1 && parse_logical(v[0], &nml->resume);
+        } else if (key == "ncubochoric") {
+            i32(&nml->ncubochoric);
+        } else if (key == "pgnum") {
+            i32(&nml->pgnum);
         } else if (key == "seed") {
             int64_t x;
             ok = v.size() == 1 && parse_int(v[0], &x);
@@ -595,17 +601,21 @@ int read_angle_file(const char* path, const char* conv, const float axisangle[4]
             memcpy(q, r, sizeof(float) * 4);
         }
     }
-    if (axisangle && axisangle[3] != 0.0f) {                          // :282-288
-        const float a[4] = {axisangle[0], axisangle[1], axisangle[2], axisangle[3] * kDtor};
-        float qax[4];
-        ax2qu(a, qax);
-        for (int64_t i = 0; i < n; ++i) {
-            float r[4];
-            quat_mult(qax, quats->data() + 4 * i, r);
-            memcpy(quats->data() + 4 * i, r, sizeof r);
-        }
-    }
+    apply_axisangle(axisangle, quats->data(), n);
     return EBSD_OK;
+}
+
+void apply_axisangle(const float axisangle[4], float* quats, int64_t n)
+{
+    if (!axisangle || axisangle[3] == 0.0f) return;                  // :282-288
+    const float a[4] = {axisangle[0], axisangle[1], axisangle[2], axisangle[3] * kDtor};
+    float qax[4];
+    ax2qu(a, qax);
+    for (int64_t i = 0; i < n; ++i) {
+        float r[4];
+        quat_mult(qax, quats + 4 * i, r);
+        memcpy(quats + 4 * i, r, sizeof r);
+    }
 }
 
 // ----------------------------------------------------------------------

@@ -69,6 +69,8 @@ private:
 int read_namelist(const char* path, ebsd_namelist* nml, std::string* err);
 int read_angle_file(const char* path, const char* conv, const float axisangle[4],
                     std::vector<float>* quats, std::string* err);
+// q <- qax (x) q for n quaternions when axisangle(4) != 0 (CTEMEBSD.f90:282-288).
+void apply_axisangle(const float axisangle[4], float* quats, int64_t n);
 int read_mc_file(const char* path, ebsd_mc_header* hdr, std::vector<int32_t>* accum_e,
                  int32_t* dst, std::string* err);
 int read_master_file(const char* path, ebsd_master_header* hdr, float* EkeVs, int32_t* atomtype,

@@ -57,12 +57,18 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
     int rc = host::read_namelist(nmlfile, &nml, &err);
     if (rc) return fail(rc, err);
 
-    // angle file (:228-288)
+    // angle file (:228-288), or a dictionary's fundamental-zone sampling
+    // (the plan of :292-298), drawn once the device is set up
     std::vector<float> quats;
-    rc = host::read_angle_file(nml.anglefile, nml.eulerconvention, nml.axisangle, &quats, &err);
-    if (rc) return fail(rc, err);
-    const int64_t numeuler = (int64_t)(quats.size() / 4);
-    say(" Number of angle entries = %lld\n", (long long)numeuler);
+    int64_t numeuler = 0;
+    const bool dictionary = nml.ncubochoric > 0;
+    if (!dictionary) {
+        rc = host::read_angle_file(nml.anglefile, nml.eulerconvention, nml.axisangle, &quats,
+                                   &err);
+        if (rc) return fail(rc, err);
+        numeuler = (int64_t)(quats.size() / 4);
+        say(" Number of angle entries = %lld\n", (long long)numeuler);
+    }
 
     // MC file (:316-367)
     say(" opening %s\n", nml.energyfile);
@@ -103,6 +109,18 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
         host::global_set_error(code, ebsd_last_error(h));
         return code;
     };
+    if (dictionary) {
+        int64_t cnt = 0;
+        rc = ebsd_sample_rfz(h, nml.ncubochoric, nml.pgnum, nullptr, nullptr, 0, &cnt);
+        if (rc) return herr(rc);
+        quats.resize((size_t)cnt * 4);
+        rc = ebsd_sample_rfz(h, nml.ncubochoric, nml.pgnum, nullptr, quats.data(), cnt, &cnt);
+        if (rc) return herr(rc);
+        host::apply_axisangle(nml.axisangle, quats.data(), cnt);
+        numeuler = cnt;
+        say(" Cubochoric sampling, %d steps, point group %d: %lld orientations in the "
+            "fundamental zone\n", nml.ncubochoric, nml.pgnum, (long long)numeuler);
+    }
     rc = ebsd_set_master(h, srtmp.data(), mh.npx, mh.npy, mh.nE, mh.numset);
     if (rc) return herr(rc);
     srtmp.clear();

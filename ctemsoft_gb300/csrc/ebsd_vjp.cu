@@ -58,8 +58,9 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     const float4 r = ldg4_keep(prm.rg + p, pol);
     float d0, d1, d2;
     rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
-    const float nd = sqrtf(fmaf(d0, d0, fmaf(d1, d1, d2 * d2)));
-    const float h0 = d0 / nd, h1 = d1 / nd, h2 = d2 / nd;
+    // derivative-only normalisation: hardware reciprocal square root
+    const float ind = rsqrtf(fmaf(d0, d0, fmaf(d1, d1, d2 * d2)));
+    const float h0 = d0 * ind, h1 = d1 * ind, h2 = d2 * ind;
     float c0 = d0, c1 = d1, c2 = d2;
     normalize_fold(c0, c1, c2);
     const float s = h2 < 0.0f ? -1.0f : 1.0f;
@@ -113,7 +114,7 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     const float gc1 = sx * dX[1] + sy * dY[1];
     const float gc2 = sx * dX[2] + sy * dY[2];
     const float pr = gc0 * h0 + gc1 * h1 + gc2 * h2;
-    const float k = s / nd;
+    const float k = s * ind;
     const float g0 = k * (gc0 - pr * h0), g1 = k * (gc1 - pr * h1), g2 = k * (gc2 - pr * h2);
     J[0] = d1 * g2 - d2 * g1;
     J[1] = d2 * g0 - d0 * g2;
@@ -136,7 +137,7 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
 // Resident CTAs per SM the register allocation is held to (256 threads
 // each); a build-time tuning knob.
 #ifndef EBSD_VJP_MIN_BLOCKS
-#define EBSD_VJP_MIN_BLOCKS 3
+#define EBSD_VJP_MIN_BLOCKS 4
 #endif
 
 template <int NV, int MODE>

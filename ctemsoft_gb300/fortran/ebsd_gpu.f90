@@ -97,6 +97,19 @@ module ebsd_gpu
       real(c_float), intent(out) :: out(*)         ! n records of (nx,ny)
     end function
 
+    ! Replaces SampleRFZ (so3.f90:267-371): rods(3,count) and quats(4,count)
+    ! of the fundamental zone of point group pgnum.  Call first with
+    ! c_null_ptr for both arrays and capacity 0 to get count.
+    integer(c_int) function ebsd_sample_rfz(h, nsteps, pgnum, rods, quats, capacity, count) &
+        bind(C, name="ebsd_sample_rfz")
+      import :: c_int, c_ptr, c_int32_t, c_int64_t
+      type(c_ptr), value :: h
+      integer(c_int32_t), value :: nsteps, pgnum
+      type(c_ptr), value :: rods, quats              ! c_loc(rods(1,1)), c_loc(quats(1,1))
+      integer(c_int64_t), value :: capacity
+      integer(c_int64_t), intent(out) :: count
+    end function
+
     integer(c_int) function ebsd_run_namelist(nmlfile, device, quiet) &
         bind(C, name="ebsd_run_namelist")
       import :: c_int, c_char

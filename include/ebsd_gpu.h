@@ -95,7 +95,10 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    num_el (:516) always uses the reference's arithmetic.
  *                    Takes effect at the next ebsd_set_detector.
  *   "tile_y"         pattern-kernel CTA height in pixels: 4, 8 (default), 16.
- *   "orient_per_cta" orientations per CTA, 1..64 (default 4). */
+ *   "orient_per_cta" orientations per CTA, 1..64 (default 4).
+ *   "vjp_tile_y"     adjoint (ebsd_vjp) CTA height: 4 or 8 (default 8;
+ *                    binning 8 always uses 8).
+ *   "vjp_orient_per_cta"  adjoint orientations per CTA, 1..64 (default 2). */
 int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value);
 
 /* Master pattern upload.  sr is the host array srtmp(-npx:npx,-npy:npy,nE,
@@ -344,6 +347,12 @@ typedef struct {
     int64_t seed;    /* default 1 */
     int32_t resume;  /* default 0; 1: keep the complete records of an existing
                         output file with the same header and compute the rest */
+    int32_t ncubochoric; /* default 0: read anglefile.  N > 0: a dictionary --
+                            the orientations are the cubochoric sampling with
+                            N steps per semi-edge of the fundamental zone of
+                            point group pgnum (ebsd_sample_rfz), the step the
+                            reference plans at CTEMEBSD.f90:292-298 */
+    int32_t pgnum;       /* default 32 (m-3m); 1..32 */
 } ebsd_namelist;
 
 /* Parse a namelist file (Fortran &EBSDdata ... / group). */

@@ -76,6 +76,7 @@ def test_namelist_defaults(lib, tmp_path):
     assert n["scalingmode"] == "not" and n["gammavalue"] == 1.0 and n["binning"] == 1
     assert n["axisangle"] == [0, 0, 0, 0]
     assert n["poisson"] == 1 and n["seed"] == 1
+    assert n["resume"] == 0 and n["ncubochoric"] == 0 and n["pgnum"] == 32
 
 
 def test_namelist_syntax(lib, tmp_path):
@@ -94,6 +95,7 @@ def test_namelist_syntax(lib, tmp_path):
         "  scalingmode = 'gamma'  ! longer than character(3): truncated\n"
         "  poisson = .false.\n"
         "  seed = 42\n"
+        "  resume = .true., ncubochoric = 50, pgnum = 24\n"
         " /\n"
         "trailing text after the group is ignored\n")
     n = capi.read_namelist(p)
@@ -105,6 +107,7 @@ def test_namelist_syntax(lib, tmp_path):
     assert n["axisangle"] == [0.5, 0.0, 1.0, 45.0]
     assert n["scalingmode"] == "gam"
     assert n["poisson"] == 0 and n["seed"] == 42
+    assert n["resume"] == 1 and n["ncubochoric"] == 50 and n["pgnum"] == 24
 
 
 @pytest.mark.parametrize("text,code", [

@@ -114,3 +114,22 @@ def test_program_noise_records_are_counts(built, tmp_path):
     hdr, recs = formats.read_output_file(tmp_path / "out.data")
     out = np.stack(recs)
     assert np.all(out == np.round(out)) and out.max() > 0
+
+
+def test_dictionary_run(built, tmp_path):
+    """ncubochoric > 0: the program samples the fundamental zone of pgnum
+    instead of reading an angle file and writes one record per sample."""
+    from oracle import oracle as O
+    wl, sr, acc, _, nml = _inputs(tmp_path, ncubochoric=5, pgnum=32, binning=1,
+                                  scalingmode="not", anglefile=str(tmp_path / "absent.txt"),
+                                  axisangle=[0.0, 0.0, 1.0, 0.0])
+    capi.run_namelist(tmp_path / "run.nml")
+    hdr, recs = formats.read_output_file(tmp_path / "out.data")
+    q = O.ro2qu(O.sample_rfz(5, 32)).astype(np.float32)
+    assert hdr == (64, 48, len(q))
+    out = np.stack(recs).reshape(len(q), 48, 64)
+    Emin, Emax = O.energy_window(16.0, 20.0, 16.0, 1.0, wl.nEbins)
+    det = O.Detector(wl.geometry(), acc, Emin, Emax)
+    ref = det.patterns_f32(sr, q, O.prefactor(15.0, 100.0, det.num_el))
+    l2, _ = rel_errors(out, ref)
+    assert l2.max() <= TOL_REF

@@ -14,6 +14,13 @@ pytestmark = pytest.mark.gpu
 ALL_GROUPS = list(range(1, 33))
 
 
+def _close_rods(rods, ref):
+    """|r| = tan(w/2): an ulp of the angle moves r by about |r|^2 ulps, so
+    vectors near 180 degrees are compared relative to that conditioning."""
+    n = np.linalg.norm(ref, axis=1, keepdims=True)
+    assert np.all(np.abs(rods - ref) <= 1e-12 * (1.0 + n) ** 2)
+
+
 def _compare(h, nsteps, pg):
     rods, quats = h.sample_rfz(nsteps, pg)
     ref = O.sample_rfz(nsteps, pg)
@@ -28,8 +35,7 @@ def test_members_and_vectors_match_oracle(built, pg):
     # C library and CUDA; membership is identical unless a point sits on a
     # zone boundary to that precision (none do on these grids)
     assert len(rods) == len(ref), (pg, len(rods), len(ref))
-    scale = np.maximum(1.0, np.abs(ref))
-    assert np.all(np.abs(rods - ref) <= 1e-12 * scale)
+    _close_rods(rods, ref)
     q64 = O.ro2qu(ref)
     assert np.abs(quats - q64).max() <= 1.2e-7
 
@@ -39,7 +45,7 @@ def test_larger_grids(built, nsteps, pg):
     h = capi.Handle(0)
     rods, quats, ref = _compare(h, nsteps, pg)
     assert len(rods) == len(ref)
-    assert np.abs(rods - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+    _close_rods(rods, ref)
 
 
 def test_buffers_capacity_and_device_pointers(built):
