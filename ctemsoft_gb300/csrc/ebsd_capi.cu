@@ -86,8 +86,8 @@ struct ebsd_handle {
     int max_persist = 0, max_window = 0;
 
     LaunchCfg cfg;
-    int vjp_tile_y = 8;  // adjoint CTA height (binning must divide it)
-    int vjp_opc = 2;     // adjoint orientations per CTA
+    int vjp_tile_y = 4;  // adjoint / Gauss-Newton CTA height (8 for binning 8)
+    int vjp_opc = 8;     // adjoint / Gauss-Newton orientations per CTA
     int weights_fp64 = 1;
     int lambert_accurate = 0;
 
@@ -1018,8 +1018,8 @@ extern "C" int ebsd_gn_accumulate(ebsd_handle* h, const float* quats, int64_t n,
     vp.drg = h->d_drg;
     vp.dW = h->d_dW;
     vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
-    vp.opc = 2;
-    const int tile_y = 8;
+    vp.opc = h->vjp_opc;
+    const int tile_y = vp.binning > h->vjp_tile_y ? 8 : h->vjp_tile_y;
     if (vp.binning > tile_y)
         return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: binning %d exceeds the tile",
                        vp.binning);

@@ -96,9 +96,11 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    Takes effect at the next ebsd_set_detector.
  *   "tile_y"         pattern-kernel CTA height in pixels: 4, 8 (default), 16.
  *   "orient_per_cta" orientations per CTA, 1..64 (default 4).
- *   "vjp_tile_y"     adjoint (ebsd_vjp) CTA height: 4 or 8 (default 8;
- *                    binning 8 always uses 8).
- *   "vjp_orient_per_cta"  adjoint orientations per CTA, 1..64 (default 2). */
+ *   "vjp_tile_y"     CTA height of ebsd_vjp and the Gauss-Newton kernels:
+ *                    4 (default) or 8; binning 8 always uses 8.
+ *   "vjp_orient_per_cta"  their orientations per CTA, 1..64 (default 8).
+ *                    (ebsd_vjp_noalloc keeps 8 and 2, the shape its size
+ *                    limit is stated for.) */
 int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value);
 
 /* Master pattern upload.  sr is the host array srtmp(-npx:npx,-npy:npy,nE,
