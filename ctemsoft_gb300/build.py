@@ -33,12 +33,13 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
              f"-I{CUDA_HOME / 'include'}"]
 
-CU_SOURCES = ["ebsd_setup.cu", "ebsd_forward.cu", "ebsd_vjp.cu", "ebsd_so3.cu", "ebsd_capi.cu"]
+CU_SOURCES = ["ebsd_setup.cu", "ebsd_forward.cu", "ebsd_vjp.cu", "ebsd_so3.cu", "ebsd_mc.cu",
+              "ebsd_capi.cu"]
 CXX_SOURCES = ["ebsd_host.cpp", "ebsd_program.cpp"]
 HEADERS = ["ebsd_internal.h", "ebsd_device.cuh", "ebsd_host.h", "ebsd_noise.cuh"]
 
 LIBNAME = "libebsdgpu.so"
-EXE = "ctemebsd"
+EXES = [("ctemebsd", "ctemebsd_main.cpp"), ("ctemmc", "ctemmc_main.cpp")]
 
 
 def _newer(src: Path, deps: list[Path], out: Path) -> bool:
@@ -66,7 +67,7 @@ def _compile(src: Path) -> Path:
 
 
 def build_library(verbose: bool = False) -> Path:
-    """Compile and link ``lib/libebsdgpu.so`` and ``lib/ctemebsd``."""
+    """Compile and link ``lib/libebsdgpu.so``, ``lib/ctemebsd`` and ``lib/ctemmc``."""
     if not Path(NVCC).exists():
         raise RuntimeError(f"nvcc not found at {NVCC}")
     OBJ.mkdir(parents=True, exist_ok=True)
@@ -76,11 +77,12 @@ def build_library(verbose: bool = False) -> Path:
     lib = LIB / LIBNAME
     if not lib.exists() or any(o.stat().st_mtime > lib.stat().st_mtime for o in objs):
         _run([NVCC, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lpthread"])
-    exe = LIB / EXE
-    main_src = CSRC / "ctemebsd_main.cpp"
-    if _newer(main_src, [lib, ROOT / "include" / "ebsd_gpu.h"], exe):
-        _run([CXX, "-O2", "-std=c++17", str(main_src), "-o", str(exe), f"-L{LIB}", "-lebsdgpu",
-              "-Wl,-rpath,$ORIGIN"])
+    for name, main in EXES:
+        exe = LIB / name
+        main_src = CSRC / main
+        if _newer(main_src, [lib, ROOT / "include" / "ebsd_gpu.h"], exe):
+            _run([CXX, "-O2", "-std=c++17", str(main_src), "-o", str(exe), f"-L{LIB}",
+                  "-lebsdgpu", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print(f"built {lib}")
     return lib
@@ -89,7 +91,8 @@ def build_library(verbose: bool = False) -> Path:
 def build_oracle() -> Path:
     """Compile the CPU oracle (test infrastructure) ``oracle/liboracle.so``."""
     out = ORACLE / "liboracle.so"
-    srcs = [ORACLE / "ebsd_oracle.c", ORACLE / "ebsd_oracle_grad.c", ORACLE / "ebsd_oracle_so3.c"]
+    srcs = [ORACLE / "ebsd_oracle.c", ORACLE / "ebsd_oracle_grad.c", ORACLE / "ebsd_oracle_so3.c",
+            ORACLE / "ebsd_oracle_mc.c"]
     if _newer(srcs[0], [*srcs[1:], ORACLE / "ebsd_oracle.h"], out):
         cc = os.environ.get("CC", "gcc")
         _run([cc, "-O3", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-std=c11",

@@ -84,6 +84,39 @@ class Namelist(C.Structure):
                 ("resume", C.c_int32), ("ncubochoric", C.c_int32), ("pgnum", C.c_int32)]
 
 
+class MCNamelist(C.Structure):
+    _fields_ = [("xtalname", C.c_char * 512), ("sig", C.c_double), ("omega", C.c_double),
+                ("numsx", C.c_int32), ("num_el", C.c_int64), ("primeseed", C.c_int32),
+                ("EkeV", C.c_double), ("dataname", C.c_char * 512), ("nthreads", C.c_int32),
+                ("Ehistmin", C.c_double), ("Ebinsize", C.c_double), ("depthmax", C.c_double),
+                ("depthstep", C.c_double), ("MCmode", C.c_char * 5), ("density", C.c_double),
+                ("Ze", C.c_double), ("at_wt", C.c_double)]
+
+
+class MCParams(C.Structure):
+    """ebsd_mc_params: namelist MCdata plus the crystal's density, average Z
+    and average atomic weight."""
+    _fields_ = [("sig", C.c_double), ("omega", C.c_double), ("EkeV", C.c_double),
+                ("Ehistmin", C.c_double), ("Ebinsize", C.c_double), ("depthmax", C.c_double),
+                ("depthstep", C.c_double), ("Ze", C.c_double), ("density", C.c_double),
+                ("at_wt", C.c_double), ("numsx", C.c_int32)]
+
+
+def mc_params(**kw) -> MCParams:
+    """MCParams with CTEMMC's namelist defaults (CTEMMC.f90:171-181) for the
+    keys not given; Ze, density and at_wt default to nickel."""
+    d = dict(sig=70.0, omega=0.0, EkeV=30.0, Ehistmin=20.0, Ebinsize=0.25, depthmax=50.0,
+             depthstep=1.0, Ze=28.0, density=8.908, at_wt=58.6934, numsx=1501)
+    d.update(kw)
+    return MCParams(**d)
+
+
+def mc_dims(p: MCParams):
+    a, b = C.c_int32(), C.c_int32()
+    _check(lib().ebsd_mc_dims(C.byref(p), C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
 _P = C.c_void_p
 _SIGS = {
     "ebsd_version": (C.c_int, []),
@@ -118,6 +151,12 @@ _SIGS = {
     "ebsd_get_detector": (C.c_int, [_P, _P, _P, _P, _P]),
     "ebsd_sample_rfz": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P, C.c_int64,
                                   C.POINTER(C.c_int64)]),
+    "ebsd_mc_dims": (C.c_int, [C.POINTER(MCParams), C.POINTER(C.c_int32),
+                               C.POINTER(C.c_int32)]),
+    "ebsd_mc_run": (C.c_int, [_P, C.POINTER(MCParams), C.c_uint64, C.c_int64, C.c_int64, _P, _P,
+                              C.POINTER(C.c_int64)]),
+    "ebsd_read_mc_namelist": (C.c_int, [C.c_char_p, C.POINTER(MCNamelist)]),
+    "ebsd_run_mc_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "ebsd_run_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "ebsd_read_mc_file": (C.c_int, [C.c_char_p, C.POINTER(MCHeader), _P]),
     "ebsd_read_master_file": (C.c_int, [C.c_char_p, C.POINTER(MasterHeader), _P, _P, _P]),
@@ -357,6 +396,24 @@ class Handle:
                self._h)
         return W, rgx, rgy, rgz
 
+    def mc_run(self, p: MCParams, seed: int, first: int, n: int, accum_e=None, accum_z=False):
+        """Monte-Carlo histograms of electrons [first, first + n).  Returns
+        (accum_e (2nx+1, 2nx+1, numEbins), accum_z or None, counted); device
+        tensors passed as accum_e / accum_z are filled in place."""
+        nE, nz = mc_dims(p)
+        nx = (p.numsx - 1) // 2
+        n10 = nx // 10
+        if accum_e is None:
+            accum_e = np.empty((2 * nx + 1, 2 * nx + 1, nE), np.int32)
+        if accum_z is True:
+            accum_z = np.empty((2 * n10 + 1, 2 * n10 + 1, nz, nE), np.int32)
+        elif accum_z is False:
+            accum_z = None
+        cnt = C.c_int64()
+        _check(lib().ebsd_mc_run(self._h, C.byref(p), seed, first, n, _ptr(accum_e),
+                                 _ptr(accum_z), C.byref(cnt)), self._h)
+        return accum_e, accum_z, cnt.value
+
     def sample_rfz(self, nsteps: int, pgnum: int):
         """Cubochoric sampling of the Rodrigues fundamental zone of point
         group pgnum (SampleRFZ).  Returns (rods (n, 3) float64, quats (n, 4)
@@ -374,6 +431,20 @@ class Handle:
 
 def run_namelist(path: str, device: int = 0, quiet: bool = True) -> None:
     _check(lib().ebsd_run_namelist(str(path).encode(), device, int(quiet)))
+
+
+def run_mc_namelist(path: str, device: int = 0, quiet: bool = True) -> None:
+    _check(lib().ebsd_run_mc_namelist(str(path).encode(), device, int(quiet)))
+
+
+def read_mc_namelist(path: str) -> dict:
+    n = MCNamelist()
+    _check(lib().ebsd_read_mc_namelist(str(path).encode(), C.byref(n)))
+    out = {}
+    for name, _ in MCNamelist._fields_:
+        v = getattr(n, name)
+        out[name] = v.decode() if isinstance(v, bytes) else v
+    return out
 
 
 def read_mc_file(path: str, with_data: bool = True):

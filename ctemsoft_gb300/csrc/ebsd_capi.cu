@@ -103,6 +103,8 @@ struct ebsd_handle {
     // fundamental-zone sampler: codes, chunk scan, device copies of outputs
     DeviceBuf rfz;
     DeviceBuf rfz_out;
+    // Monte-Carlo histograms staged for host outputs, and the counter
+    DeviceBuf mc;
 };
 
 namespace {
@@ -351,6 +353,7 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
     cudaFree(h->batch_table.ptr);
     cudaFree(h->rfz.ptr);
     cudaFree(h->rfz_out.ptr);
+    cudaFree(h->mc.ptr);
     if (h->batch_table_host) cudaFreeHost(h->batch_table_host);
     if (h->batch_exec) cudaGraphExecDestroy(h->batch_exec);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -1662,5 +1665,69 @@ extern "C" int ebsd_sample_rfz(ebsd_handle* h, int32_t nsteps, int32_t pgnum, do
         CK(h, cudaMemcpy(quats, d_quats, sizeof(float) * 4 * (size_t)w, cudaMemcpyDeviceToHost),
            "quaternion copy");
     *count = n;
+    return EBSD_OK;
+}
+
+// ----------------------------------------------------------------------
+// Monte-Carlo backscatter histograms (CTEMMC.f90:307-529)
+
+extern "C" int ebsd_mc_dims(const ebsd_mc_params* p, int32_t* numEbins, int32_t* numzbins)
+{
+    if (!p || !numEbins || !numzbins) return set_err(nullptr, EBSD_EINVAL, "ebsd_mc_dims: null");
+    const bool ok = std::isfinite(p->EkeV) && std::isfinite(p->Ehistmin) &&
+                    p->Ebinsize > 0.0 && p->depthstep > 0.0 && p->depthmax >= 0.0 &&
+                    p->EkeV > p->Ehistmin && p->numsx >= 3 && (p->numsx % 2) == 1 &&
+                    p->numsx <= 20001 && (p->EkeV - p->Ehistmin) / p->Ebinsize < 1.0e5 &&
+                    p->depthmax / p->depthstep < 1.0e5;
+    if (!ok)
+        return set_err(nullptr, EBSD_EINVAL,
+                       "Monte-Carlo parameters: need EkeV > Ehistmin, Ebinsize > 0, depthstep > "
+                       "0, odd numsx in 3..20001");
+    *numEbins = (int32_t)((p->EkeV - p->Ehistmin) / p->Ebinsize) + 1;
+    *numzbins = (int32_t)(p->depthmax / p->depthstep) + 1;
+    return EBSD_OK;
+}
+
+extern "C" int ebsd_mc_run(ebsd_handle* h, const ebsd_mc_params* p, uint64_t seed,
+                           int64_t first_electron, int64_t n_electrons, int32_t* accum_e,
+                           int32_t* accum_z, int64_t* counted)
+{
+    if (!h) return set_err(nullptr, EBSD_EINVAL, "null handle");
+    if (!p || !accum_e) return set_err(h, EBSD_EINVAL, "ebsd_mc_run: null argument");
+    int32_t nE = 0, nz = 0;
+    if (ebsd_mc_dims(p, &nE, &nz) != EBSD_OK) return set_err(h, EBSD_EINVAL, "%s", g_err.c_str());
+    if (!(p->Ze > 0.0) || !(p->density > 0.0) || !(p->at_wt > 0.0) || !std::isfinite(p->sig) ||
+        !std::isfinite(p->omega) || std::fabs(p->omega) >= 90.0)
+        return set_err(h, EBSD_EINVAL, "ebsd_mc_run: Ze, density, at_wt must be > 0, tilts finite");
+    if (n_electrons < 0 || first_electron < 0)
+        return set_err(h, EBSD_EINVAL, "ebsd_mc_run: negative electron range");
+    int rc = activate(h);
+    if (rc) return rc;
+    const McConsts K = mc_constants(*p);
+    const size_t ne = (size_t)nE * p->numsx * p->numsx;
+    const size_t w10 = 2 * (size_t)K.nz10 + 1;
+    const size_t nzs = (size_t)nE * nz * w10 * w10;
+    const bool edev = ptr_kind(accum_e) == kDevice;
+    const bool zdev = accum_z ? ptr_kind(accum_z) == kDevice : true;
+    const size_t o_cnt = 0, o_e = 256;
+    const size_t o_z = o_e + (edev ? 0 : ((ne * 4 + 255) & ~size_t(255)));
+    rc = ensure(h, h->mc, o_z + (zdev ? 0 : nzs * 4) + 256, "Monte-Carlo histograms");
+    if (rc) return rc;
+    char* base = (char*)h->mc.ptr;
+    int32_t* de = edev ? accum_e : (int32_t*)(base + o_e);
+    int32_t* dz = accum_z ? (zdev ? accum_z : (int32_t*)(base + o_z)) : nullptr;
+    unsigned long long* dcnt = (unsigned long long*)(base + o_cnt);
+    cudaStream_t s = h->stream;
+    CK(h, cudaMemsetAsync(de, 0, ne * 4, s), "histogram clear");
+    if (dz) CK(h, cudaMemsetAsync(dz, 0, nzs * 4, s), "histogram clear");
+    CK(h, cudaMemsetAsync(dcnt, 0, sizeof(unsigned long long), s), "counter clear");
+    CK(h, launch_mc(K, seed, first_electron, n_electrons, de, dz, dcnt, s), "Monte-Carlo kernel");
+    unsigned long long c = 0;
+    CK(h, cudaMemcpyAsync(&c, dcnt, sizeof c, cudaMemcpyDeviceToHost, s), "counter copy");
+    if (!edev) CK(h, cudaMemcpyAsync(accum_e, de, ne * 4, cudaMemcpyDeviceToHost, s), "accum_e copy");
+    if (accum_z && !zdev)
+        CK(h, cudaMemcpyAsync(accum_z, dz, nzs * 4, cudaMemcpyDeviceToHost, s), "accum_z copy");
+    CK(h, cudaStreamSynchronize(s), "Monte-Carlo");
+    if (counted) *counted = (int64_t)c;
     return EBSD_OK;
 }

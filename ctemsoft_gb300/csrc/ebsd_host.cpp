@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <sstream>
 
 namespace ebsd {
@@ -354,37 +355,14 @@ bool expand_values(const std::vector<Tok>& vals, std::vector<std::string>* out)
     return true;
 }
 
-}  // namespace
+// One namelist group (Fortran namelist input): calls assign(key, index,
+// values) for every "name[(index)] = values" of &group ... / in order; index
+// is -1 without a subscript.  assign returns EBSD_OK or an error code.
+using Assign =
+    std::function<int(const std::string&, int64_t, const std::vector<std::string>&)>;
 
-int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
+int parse_group(const char* path, const char* group, const Assign& assign, std::string* err)
 {
-    // defaults of CTEMEBSD.f90:179-198
-    memset(nml, 0, sizeof *nml);
-    nml->L = 20000.0f;
-    nml->thetac = 0.0f;
-    nml->delta = 25.0f;
-    nml->numsx = 640;
-    nml->numsy = 480;
-    nml->xpc = 0.0f;
-    nml->ypc = 0.0f;
-    nml->energymin = 15.0f;
-    nml->energymax = 30.0f;
-    snprintf(nml->anglefile, sizeof nml->anglefile, "euler.txt");
-    snprintf(nml->eulerconvention, sizeof nml->eulerconvention, "tsl");
-    snprintf(nml->FZfile, sizeof nml->FZfile, "FZ.data");
-    snprintf(nml->energyfile, sizeof nml->energyfile, "energy.data");
-    snprintf(nml->datafile, sizeof nml->datafile, "EBSDout.data");
-    nml->beamcurrent = 14.513;
-    nml->dwelltime = 100.0;
-    snprintf(nml->scalingmode, sizeof nml->scalingmode, "not");
-    nml->gammavalue = 1.0f;
-    nml->binning = 1;
-    nml->poisson = 1;
-    nml->seed = 1;
-    nml->resume = 0;
-    nml->ncubochoric = 0;
-    nml->pgnum = 32;
-
     std::ifstream in(path ? path : "");
     if (!in) {
         *err = std::string("cannot open namelist file '") + (path ? path : "") + "'";
@@ -394,15 +372,16 @@ int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
     ss << in.rdbuf();
     const std::vector<Tok> toks = tokenize(ss.str());
     size_t i = 0;
-    // find the group start &EBSDdata (or $EBSDdata)
+    // find the group start &group (or $group)
+    const std::string g = lower(group);
     for (; i < toks.size(); ++i) {
         if (toks[i].kind == Tok::Word) {
             const std::string w = lower(toks[i].text);
-            if (w == "&ebsddata" || w == "$ebsddata") break;
+            if (w == "&" + g || w == "$" + g) break;
         }
     }
     if (i >= toks.size() || toks[i].kind == Tok::End) {
-        *err = "namelist group &EBSDdata not found in '" + std::string(path) + "'";
+        *err = "namelist group &" + std::string(group) + " not found in '" + std::string(path) + "'";
         return EBSD_EFORMAT;
     }
     ++i;
@@ -453,6 +432,44 @@ int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
             *err = "namelist: no value for '" + key + "'";
             return EBSD_EFORMAT;
         }
+        const int rc = assign(key, index, v);
+        if (rc) return rc;
+    }
+    return EBSD_OK;
+}
+
+}  // namespace
+
+int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
+{
+    // defaults of CTEMEBSD.f90:179-198
+    memset(nml, 0, sizeof *nml);
+    nml->L = 20000.0f;
+    nml->thetac = 0.0f;
+    nml->delta = 25.0f;
+    nml->numsx = 640;
+    nml->numsy = 480;
+    nml->xpc = 0.0f;
+    nml->ypc = 0.0f;
+    nml->energymin = 15.0f;
+    nml->energymax = 30.0f;
+    snprintf(nml->anglefile, sizeof nml->anglefile, "euler.txt");
+    snprintf(nml->eulerconvention, sizeof nml->eulerconvention, "tsl");
+    snprintf(nml->FZfile, sizeof nml->FZfile, "FZ.data");
+    snprintf(nml->energyfile, sizeof nml->energyfile, "energy.data");
+    snprintf(nml->datafile, sizeof nml->datafile, "EBSDout.data");
+    nml->beamcurrent = 14.513;
+    nml->dwelltime = 100.0;
+    snprintf(nml->scalingmode, sizeof nml->scalingmode, "not");
+    nml->gammavalue = 1.0f;
+    nml->binning = 1;
+    nml->poisson = 1;
+    nml->seed = 1;
+    nml->resume = 0;
+    nml->ncubochoric = 0;
+    nml->pgnum = 32;
+    return parse_group(path, "EBSDdata", [&](const std::string& key, int64_t index,
+                                             const std::vector<std::string>& v) -> int {
         bool ok = true;
         auto f32 = [&](float* dst) { ok = v.size() == 1 && parse_real_f(v[0], dst); };
         auto f64 = [&](double* dst) { ok = v.size() == 1 && parse_real_d(v[0], dst); };
@@ -509,8 +526,67 @@ int read_namelist(const char* path, ebsd_namelist* nml, std::string* err)
             *err = "namelist: bad value for '" + key + "'";
             return EBSD_EFORMAT;
         }
-    }
-    return EBSD_OK;
+        return EBSD_OK;
+    }, err);
+}
+
+int read_mc_namelist(const char* path, ebsd_mc_namelist* nml, std::string* err)
+{
+    // defaults of CTEMMC.f90:171-183
+    memset(nml, 0, sizeof *nml);
+    snprintf(nml->MCmode, sizeof nml->MCmode, "CSDA");
+    snprintf(nml->xtalname, sizeof nml->xtalname, "undefined");
+    nml->sig = 70.0;
+    nml->omega = 0.0;
+    nml->numsx = 1501;
+    nml->primeseed = 932117;
+    nml->num_el = 10000000;
+    nml->nthreads = 4;
+    nml->EkeV = 30.0;
+    nml->Ehistmin = 30.0 - 10.0;  // EkeV - 10 with the default EkeV, before the read
+    nml->Ebinsize = 0.25;
+    nml->depthmax = 50.0;
+    nml->depthstep = 1.0;
+    snprintf(nml->dataname, sizeof nml->dataname, "undefined.data");
+    return parse_group(path, "MCdata", [&](const std::string& key, int64_t,
+                                           const std::vector<std::string>& v) -> int {
+        bool ok = true;
+        auto f64 = [&](double* dst) { ok = v.size() == 1 && parse_real_d(v[0], dst); };
+        auto i32 = [&](int32_t* dst) {
+            int64_t x;
+            ok = v.size() == 1 && parse_int(v[0], &x) && x >= INT32_MIN && x <= INT32_MAX;
+            if (ok) *dst = (int32_t)x;
+        };
+        if (key == "xtalname") set_str(nml->xtalname, sizeof nml->xtalname, v[0], 132);
+        else if (key == "sig") f64(&nml->sig);
+        else if (key == "omega") f64(&nml->omega);
+        else if (key == "numsx") i32(&nml->numsx);
+        else if (key == "num_el") {
+            int64_t x;
+            ok = v.size() == 1 && parse_int(v[0], &x);
+            if (ok) nml->num_el = x;
+        } else if (key == "primeseed") i32(&nml->primeseed);
+        else if (key == "ekev") f64(&nml->EkeV);
+        else if (key == "dataname") set_str(nml->dataname, sizeof nml->dataname, v[0], 60);
+        else if (key == "nthreads") i32(&nml->nthreads);
+        else if (key == "ehistmin") f64(&nml->Ehistmin);
+        else if (key == "ebinsize") f64(&nml->Ebinsize);
+        else if (key == "depthmax") f64(&nml->depthmax);
+        else if (key == "depthstep") f64(&nml->depthstep);
+        else if (key == "mcmode") set_str(nml->MCmode, sizeof nml->MCmode, v[0], 4);
+        else if (key == "density") f64(&nml->density);
+        else if (key == "ze") f64(&nml->Ze);
+        else if (key == "at_wt") f64(&nml->at_wt);
+        else {
+            *err = "namelist: unknown variable '" + key + "' in group MCdata";
+            return EBSD_EFORMAT;
+        }
+        if (!ok) {
+            *err = "namelist: bad value for '" + key + "'";
+            return EBSD_EFORMAT;
+        }
+        return EBSD_OK;
+    }, err);
 }
 
 // ----------------------------------------------------------------------
@@ -786,6 +862,15 @@ extern "C" int ebsd_read_namelist(const char* path, ebsd_namelist* nml)
     if (!nml) return host::global_set_error(EBSD_EINVAL, "ebsd_read_namelist: null output");
     std::string err;
     int rc = host::read_namelist(path, nml, &err);
+    if (rc) host::global_set_error(rc, err.c_str());
+    return rc;
+}
+
+extern "C" int ebsd_read_mc_namelist(const char* path, ebsd_mc_namelist* nml)
+{
+    if (!nml) return host::global_set_error(EBSD_EINVAL, "ebsd_read_mc_namelist: null output");
+    std::string err;
+    int rc = host::read_mc_namelist(path, nml, &err);
     if (rc) host::global_set_error(rc, err.c_str());
     return rc;
 }

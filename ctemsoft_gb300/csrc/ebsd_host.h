@@ -67,6 +67,7 @@ private:
 };
 
 int read_namelist(const char* path, ebsd_namelist* nml, std::string* err);
+int read_mc_namelist(const char* path, ebsd_mc_namelist* nml, std::string* err);
 int read_angle_file(const char* path, const char* conv, const float axisangle[4],
                     std::vector<float>* quats, std::string* err);
 // q <- qax (x) q for n quaternions when axisangle(4) != 0 (CTEMEBSD.f90:282-288).

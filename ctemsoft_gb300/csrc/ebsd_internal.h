@@ -162,4 +162,16 @@ cudaError_t launch_rfz(const So3Consts& K, const double* xs, int m, int type, in
                        long long* count, long long cap, double* rods, float* quats,
                        bool count_only, cudaStream_t s);
 
+// Monte-Carlo backscatter histograms (ebsd_mc.cu): CTEMMC.f90:410-440
+// derived constants.
+struct McConsts {
+    double EkeV, Ehistmin, Ebinsize, depthstep, Ze, Emin, pre, prealpha, J, predEds, tpi, tano,
+        delta, sPi2, cxstart, czstart;
+    int nx, nz10, numEbins, numzbins;
+};
+McConsts mc_constants(const ebsd_mc_params& p);
+cudaError_t launch_mc(const McConsts& K, uint64_t seed, long long e0, long long n,
+                      int32_t* accum_e, int32_t* accum_z, unsigned long long* counted,
+                      cudaStream_t s);
+
 }  // namespace ebsd

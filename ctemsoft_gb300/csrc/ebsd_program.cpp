@@ -245,3 +245,97 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
     say("  Time per step/pixel [s] %10.6f\n", numeuler > 0 ? secs / (double)numeuler : 0.0);
     return EBSD_OK;
 }
+
+// The CTEMMC program on the GPU: CTEMMC.f90:48-277, the trajectory loop of
+// single_run replaced by ebsd_mc_run, the MC file written as the reference
+// writes it.
+extern "C" int ebsd_run_mc_namelist(const char* nmlfile, int device, int quiet)
+{
+    auto say = [&](const char* fmt, auto... args) {
+        if (!quiet) {
+            printf(fmt, args...);
+            fflush(stdout);
+        }
+    };
+    say(" CTEMMC (GB300): Monte Carlo Electron Trajectory Simulation for EBSD+Lambert\n");
+    ebsd_mc_namelist nml;
+    std::string err;
+    int rc = host::read_mc_namelist(nmlfile, &nml, &err);
+    if (rc) return fail(rc, err);
+    if (std::string(nml.xtalname) == "undefined")                       // :188-190
+        return fail(EBSD_EINVAL, std::string("CTEMMC: structure file name is undefined in ") +
+                                     nmlfile);
+    if (std::string(nml.MCmode) != "CSDA")
+        return fail(EBSD_EUNSUPPORTED, std::string("MCmode '") + nml.MCmode +
+                                           "': only 'CSDA' exists in the reference");
+    if (!(nml.density > 0.0) || !(nml.Ze > 0.0) || !(nml.at_wt > 0.0))
+        return fail(EBSD_EUNSUPPORTED,
+                    std::string("reading crystal files is not supported: give density, Ze and "
+                                "at_wt in &MCdata (CTEMMC prints them as 'Density, avZ, avA' for ") +
+                        nml.xtalname + ")");
+    if (nml.num_el < 0 || nml.nthreads < 1) return fail(EBSD_EINVAL, "num_el, nthreads");
+    say(" Density, avZ, avA = %10.5f%10.5f,%10.5f\n", nml.density, nml.Ze, nml.at_wt);
+    ebsd_mc_params p;
+    p.sig = nml.sig;
+    p.omega = nml.omega;
+    p.EkeV = nml.EkeV;
+    p.Ehistmin = nml.Ehistmin;
+    p.Ebinsize = nml.Ebinsize;
+    p.depthmax = nml.depthmax;
+    p.depthstep = nml.depthstep;
+    p.Ze = nml.Ze;
+    p.density = nml.density;
+    p.at_wt = nml.at_wt;
+    p.numsx = nml.numsx;
+    int32_t nE = 0, nz = 0;
+    rc = ebsd_mc_dims(&p, &nE, &nz);
+    if (rc) return rc;
+    const int nx = (nml.numsx - 1) / 2, n10 = nx / 10;
+    std::vector<int32_t> accum_e((size_t)nE * nml.numsx * nml.numsx);
+    std::vector<int32_t> accum_z((size_t)nE * nz * (2 * n10 + 1) * (2 * n10 + 1));
+    HandleGuard hg;
+    rc = ebsd_create(&hg.h, device);
+    if (rc) return rc;
+    const int64_t total = nml.num_el * (int64_t)nml.nthreads;
+    say(" electrons: %lld x %d streams of the reference = %lld, one Philox stream each\n",
+        (long long)nml.num_el, nml.nthreads, (long long)total);
+    const auto t0 = std::chrono::steady_clock::now();
+    int64_t counted = 0;
+    rc = ebsd_mc_run(hg.h, &p, (uint64_t)(uint32_t)nml.primeseed, 0, total, accum_e.data(),
+                     accum_z.data(), &counted);
+    if (rc) {
+        host::global_set_error(rc, ebsd_last_error(hg.h));
+        return rc;
+    }
+    const double secs =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    say("\n  All trajectories complete (%.3f s); saving data to file %s\n\n", secs,
+        nml.dataname);
+    say("  Total number of electrons generated = %lld\n", (long long)total);
+    say("  Number of electrons on detector       = %lld\n", (long long)counted);
+
+    host::FortranWriter out(nml.dataname);                              // :259-277
+    if (!out.ok()) return fail(EBSD_EIO, std::string("cannot create ") + nml.dataname);
+    auto chars = [](const char* sv, size_t n) {
+        std::string r(sv);
+        r.resize(n, ' ');
+        return r;
+    };
+    const std::string prog = chars("CTEMMC.f90", 132), ver = chars("2.0/2013", 8),
+                      xtal = chars(nml.xtalname, 132), mode = chars(nml.MCmode, 4);
+    struct __attribute__((packed)) {
+        int32_t a, b, c, d;
+        int64_t n;
+        int32_t t;
+    } dims = {nE, nz, nml.numsx, nml.numsx, total, nml.nthreads};
+    const double ener[5] = {nml.EkeV, nml.Ehistmin, nml.Ebinsize, nml.depthmax, nml.depthstep};
+    const double tilt[2] = {nml.sig, nml.omega};
+    bool ok = out.write(prog.data(), prog.size()) && out.write(ver.data(), ver.size()) &&
+              out.write(xtal.data(), xtal.size()) && out.write(&dims, sizeof dims) &&
+              out.write(ener, sizeof ener) && out.write(tilt, sizeof tilt) &&
+              out.write(mode.data(), mode.size()) &&
+              out.write(accum_e.data(), accum_e.size() * 4) &&
+              out.write(accum_z.data(), accum_z.size() * 4);
+    if (!ok || !out.close()) return fail(EBSD_EIO, "MC output file write failed");
+    return EBSD_OK;
+}

@@ -150,8 +150,13 @@ __global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
     float* tile = sm;
     float* red = sm + 33 * tile_y;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
-    const int t = (int)(blockIdx.x % (unsigned)ntiles);
-    const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
+    // Orientation blocks vary fastest across the grid: the CTAs resident at
+    // any moment cover a few tiles for many orientations, so each tile's
+    // per-pixel tables (W, dW, rg, drg: larger than L2 together with the
+    // master at 640x480) are read from DRAM about once, not once per sweep.
+    const unsigned n_ob = (unsigned)((prm.n + opc - 1) / opc);
+    const int t = (int)(blockIdx.x / n_ob);
+    const int64_t o_begin = (int64_t)(blockIdx.x % n_ob) * opc;
     const int x = (t % tiles_x) * kTileX + tx;
     const int y = (t / tiles_x) * tile_y + ty;
     const int b = vp.binning;
@@ -287,8 +292,13 @@ __global__ void __launch_bounds__(256, 2) k_gn(const FwdParams prm, const VjpPar
     float* jt = sm + 33 * tile_y;
     float* red = jt + 6 * 33 * tile_y;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
-    const int t = (int)(blockIdx.x % (unsigned)ntiles);
-    const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
+    // Orientation blocks vary fastest across the grid: the CTAs resident at
+    // any moment cover a few tiles for many orientations, so each tile's
+    // per-pixel tables (W, dW, rg, drg: larger than L2 together with the
+    // master at 640x480) are read from DRAM about once, not once per sweep.
+    const unsigned n_ob = (unsigned)((prm.n + opc - 1) / opc);
+    const int t = (int)(blockIdx.x / n_ob);
+    const int64_t o_begin = (int64_t)(blockIdx.x % n_ob) * opc;
     const int x = (t % tiles_x) * kTileX + tx;
     const int y = (t / tiles_x) * tile_y + ty;
     const int b = vp.binning;

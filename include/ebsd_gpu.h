@@ -296,6 +296,77 @@ int ebsd_sample_rfz(ebsd_handle* h, int32_t nsteps, int32_t pgnum, double* rods,
                     int64_t capacity, int64_t* count);
 
 /* ------------------------------------------------------------------ */
+/* Monte-Carlo backscatter histograms (the MC file's accum_e / accum_z) */
+/* ------------------------------------------------------------------ */
+
+/* Parameters of CTEMMC's namelist MCdata (CTEMMC.f90:165-181) plus the
+ * three material numbers the reference derives from the crystal file with
+ * CalcDensity (:196-202); CTEMMC prints them as "Density, avZ, avA". */
+typedef struct {
+    double sig;       /* sample tilt about TD [deg] */
+    double omega;     /* sample tilt about RD [deg] */
+    double EkeV;      /* beam energy [keV] */
+    double Ehistmin;  /* lowest energy bin [keV] */
+    double Ebinsize;  /* energy bin width [keV] */
+    double depthmax;  /* deepest exit-depth bin [nm] */
+    double depthstep; /* exit-depth bin width [nm] */
+    double Ze;        /* average atomic number */
+    double density;   /* [g/cm^3] */
+    double at_wt;     /* average atomic weight [g/mol] */
+    int32_t numsx;    /* Lambert points per side, odd; nx = (numsx-1)/2 */
+} ebsd_mc_params;
+
+/* numEbins = int((EkeV-Ehistmin)/Ebinsize)+1, numzbins = int(depthmax/
+ * depthstep)+1 (CTEMMC.f90:205-206); EBSD_EINVAL for inconsistent values. */
+int ebsd_mc_dims(const ebsd_mc_params* p, int32_t* numEbins, int32_t* numzbins);
+
+/* Replaces single_run (CTEMMC.f90:307-529, CSDA mode) for electrons
+ * [first_electron, first_electron + n_electrons): each electron's random
+ * numbers come from its own Philox4x32-10 stream keyed by `seed` (the
+ * reference's sequential streams cannot be split across a GPU), mapped to
+ * the reference's single-precision uniforms; results depend only on seed
+ * and the electron range, so ranges run on several GPUs sum to the
+ * single-GPU histogram.  Overwrites
+ *   accum_e  numEbins x numsx x numsx int32, Fortran accum_e(E, x, y);
+ *   accum_z  numEbins x numzbins x (2(nx/10)+1)^2 int32 (may be NULL);
+ * (host or device pointers) and sets *counted (may be NULL) to the number of
+ * electrons recorded in accum_e.  Exits whose energy bin or coarse depth
+ * pixel would fall outside the arrays, which the reference writes past, are
+ * dropped. */
+int ebsd_mc_run(ebsd_handle* h, const ebsd_mc_params* p, uint64_t seed, int64_t first_electron,
+                int64_t n_electrons, int32_t* accum_e, int32_t* accum_z, int64_t* counted);
+
+/* Parsed &MCdata namelist with the defaults of CTEMMC.f90:171-183 (Ehistmin
+ * defaults to 20, the reference's EkeV - 10 evaluated before the namelist is
+ * read). */
+typedef struct {
+    char xtalname[512];
+    double sig, omega;
+    int32_t numsx;
+    int64_t num_el;     /* electrons per thread; the run uses num_el*nthreads */
+    int32_t primeseed;  /* the Philox seed here */
+    double EkeV;
+    char dataname[512];
+    int32_t nthreads;
+    double Ehistmin, Ebinsize, depthmax, depthstep;
+    char MCmode[5];
+    /* keys this library adds: the crystal's density [g/cm^3], average Z and
+     * average atomic weight [g/mol], which the reference computes from the
+     * crystal file (CalcDensity, CTEMMC.f90:196-202); reading crystal files
+     * is outside this library, so they are required (default 0 = not set) */
+    double density, Ze, at_wt;
+} ebsd_mc_namelist;
+
+/* Parse a namelist file (&MCdata ... / group). */
+int ebsd_read_mc_namelist(const char* path, ebsd_mc_namelist* nml);
+
+/* The whole CTEMMC program (CTEMMC.f90:48-277) for namelist file `nmlfile`
+ * on device `device`: num_el*nthreads electrons, the MC file of
+ * CTEMMC.f90:262-277 (the format ebsd_read_mc_file reads).  Prints the
+ * reference's progress lines unless quiet != 0. */
+int ebsd_run_mc_namelist(const char* nmlfile, int device, int quiet);
+
+/* ------------------------------------------------------------------ */
 /* File formats and the drop-in program                                 */
 /* ------------------------------------------------------------------ */
 

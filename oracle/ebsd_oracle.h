@@ -92,6 +92,21 @@ int oracle_fz_code(const double rod[3], int type, int order);
 int64_t oracle_rfz_axis(int nsteps, double* xs, int64_t cap);
 int64_t oracle_sample_rfz(int nsteps, int pgnum, double* rods, int64_t cap);
 
+/* Monte-Carlo backscatter histogram, CTEMMC.f90:307-529 (ebsd_oracle_mc.c).
+ * Material numbers are CalcDensity's density [g/cm^3], average Z and
+ * average atomic weight [g/mol]. */
+typedef struct {
+    double sig, omega, EkeV, Ehistmin, Ebinsize, depthmax, depthstep;
+    double Ze, density, at_wt;
+    int32_t numsx; /* odd number of Lambert points per side */
+} oracle_mc_params;
+int oracle_mc_dims(const oracle_mc_params* p, int* numEbins, int* numzbins);
+int64_t oracle_mc_philox(const oracle_mc_params* p, uint64_t seed, int64_t e0, int64_t e1,
+                         int32_t* accum_e, int32_t* accum_z);
+int64_t oracle_mc_reference_rng(const oracle_mc_params* p, int32_t primeseed, int nthreads,
+                                int64_t num_el, int32_t* accum_e, int32_t* accum_z);
+void oracle_mc_uniforms(int kind, uint64_t seed_or_prime, int64_t electron, int count, float* u);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,6 +78,10 @@ _SIGS = {
     "oracle_fz_code": (C.c_int, [_P, C.c_int, C.c_int]),
     "oracle_rfz_axis": (C.c_int64, [C.c_int, _P, C.c_int64]),
     "oracle_sample_rfz": (C.c_int64, [C.c_int, C.c_int, _P, C.c_int64]),
+    "oracle_mc_dims": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "oracle_mc_philox": (C.c_int64, [_P, C.c_uint64, C.c_int64, C.c_int64, _P, _P]),
+    "oracle_mc_reference_rng": (C.c_int64, [_P, C.c_int32, C.c_int, C.c_int64, _P, _P]),
+    "oracle_mc_uniforms": (None, [C.c_int, C.c_uint64, C.c_int64, C.c_int, _P]),
 }
 
 _lib = None
@@ -85,7 +89,7 @@ _lib = None
 
 def build() -> Path:
     srcs = [HERE / n for n in ("ebsd_oracle.c", "ebsd_oracle_grad.c", "ebsd_oracle_so3.c",
-                               "ebsd_oracle.h")]
+                               "ebsd_oracle_mc.c", "ebsd_oracle.h")]
     if not LIB.exists() or LIB.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
         subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
     return LIB
@@ -386,3 +390,56 @@ def sample_rfz(nsteps, pgnum):
     rods = np.zeros((max(n, 1), 3))
     lib().oracle_sample_rfz(nsteps, pgnum, _p(rods), n)
     return rods[:n]
+
+
+# ---------------------------------------------------------------------------
+# Monte-Carlo backscatter histogram (ebsd_oracle_mc.c)
+
+class MCParams(C.Structure):
+    _fields_ = [("sig", C.c_double), ("omega", C.c_double), ("EkeV", C.c_double),
+                ("Ehistmin", C.c_double), ("Ebinsize", C.c_double), ("depthmax", C.c_double),
+                ("depthstep", C.c_double), ("Ze", C.c_double), ("density", C.c_double),
+                ("at_wt", C.c_double), ("numsx", C.c_int32)]
+
+
+def mc_params(**kw) -> MCParams:
+    d = dict(sig=70.0, omega=0.0, EkeV=20.0, Ehistmin=10.0, Ebinsize=1.0, depthmax=100.0,
+             depthstep=1.0, Ze=28.0, density=8.9, at_wt=58.69, numsx=101)
+    d.update(kw)
+    return MCParams(**d)
+
+
+def mc_dims(p: MCParams):
+    a, b = C.c_int(), C.c_int()
+    if lib().oracle_mc_dims(C.byref(p), C.byref(a), C.byref(b)):
+        raise ValueError("bad Monte-Carlo parameters")
+    return a.value, b.value
+
+
+def _mc_arrays(p):
+    nE, nz = mc_dims(p)
+    nx = (p.numsx - 1) // 2
+    n10 = nx // 10
+    acc = np.zeros((2 * nx + 1, 2 * nx + 1, nE), np.int32)          # Fortran (E, x, y)
+    accz = np.zeros((2 * n10 + 1, 2 * n10 + 1, nz, nE), np.int32)   # Fortran (E, z, x, y)
+    return acc, accz
+
+
+def mc_philox(p: MCParams, seed: int, e0: int, e1: int):
+    """Histograms of electrons [e0, e1) on the GPU's Philox stream."""
+    acc, accz = _mc_arrays(p)
+    n = lib().oracle_mc_philox(C.byref(p), seed, e0, e1, _p(acc), _p(accz))
+    return acc, accz, n
+
+
+def mc_reference_rng(p: MCParams, primeseed: int, nthreads: int, num_el: int):
+    """Histograms with the reference's own generator streams."""
+    acc, accz = _mc_arrays(p)
+    n = lib().oracle_mc_reference_rng(C.byref(p), primeseed, nthreads, num_el, _p(acc), _p(accz))
+    return acc, accz, n
+
+
+def mc_uniforms(kind: int, seed: int, electron: int, count: int):
+    u = np.zeros(count, np.float32)
+    lib().oracle_mc_uniforms(kind, seed, electron, count, _p(u))
+    return u
