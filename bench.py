@@ -52,7 +52,7 @@ def _args():
     ap.add_argument("--vjp-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "mc"],
                     help="c2: 640x480 plain forward (default); c3: 64-job batch; "
                          "c5: Gauss-Newton refinement")
     ap.add_argument("--c3-jobs", type=int, default=64,
@@ -60,6 +60,8 @@ def _args():
     ap.add_argument("--c3-max-orient", type=int, default=0,
                     help="c3: cap each job's orientation count (0: no cap)")
     ap.add_argument("--gn-orient", type=int, default=100000)
+    ap.add_argument("--mc-electrons", type=int, default=20000000,
+                    help="mc: electrons per timed step")
     ap.add_argument("--fd-iters", type=int, default=3)
     return ap.parse_args()
 
@@ -642,6 +644,89 @@ def run_gn(args):
     return 0
 
 
+def run_mc(args):
+    """Monte-Carlo backscatter histograms (CTEMMC) at the program's defaults:
+    Ni, 30 keV beam, 70 deg tilt, 1501^2 Lambert grid, 0.25 keV bins from
+    20 keV (41 bins), exit depth to 50 nm.  value: electrons/s with the
+    histograms resident on the device; e2e: the same through the C ABI into
+    host arrays (370 MB copied back per step); cpu_baseline: the oracle's
+    restatement with the reference's own generator streams, one OpenMP
+    thread per stream as the reference runs it, on all host cores."""
+    import numpy as np
+    import torch
+
+    from ctemsoft_gb300 import capi
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    p = capi.mc_params(Ze=28.0, density=8.908, at_wt=58.6934)
+    nE, nz = capi.mc_dims(p)
+    n10 = 750 // 10
+    h = capi.Handle(0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    h.set_stream(stream.cuda_stream)
+    de = torch.empty((1501, 1501, nE), dtype=torch.int32, device=dev)
+    dz = torch.empty((2 * n10 + 1, 2 * n10 + 1, nz, nE), dtype=torch.int32, device=dev)
+    N = args.mc_electrons
+    for w in range(args.warmup):
+        h.mc_run(p, 1000 + w, 0, max(1, N // 10), accum_e=de, accum_z=dz)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    counted = 0
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        _, _, c = h.mc_run(p, 932117, k * N, N, accum_e=de, accum_z=dz)
+        ev[k][1].record(stream)
+        counted += c
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    value = N / (ms / 1e3)
+    # end to end: host histograms
+    he = np.empty((1501, 1501, nE), np.int32)
+    hz = np.empty((2 * n10 + 1, 2 * n10 + 1, nz, nE), np.int32)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.e2e_steps, 2))
+    for k in range(e2e_steps):
+        h.mc_run(p, 932117, k * N, N, accum_e=he, accum_z=hz)
+    e2e = e2e_steps * N / (time.perf_counter() - t0)
+    base = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        threads = O.max_threads()
+        op = O.mc_params(sig=p.sig, omega=p.omega, EkeV=p.EkeV, Ehistmin=p.Ehistmin,
+                         Ebinsize=p.Ebinsize, depthmax=p.depthmax, depthstep=p.depthstep,
+                         Ze=p.Ze, density=p.density, at_wt=p.at_wt, numsx=p.numsx)
+        t = time.perf_counter()
+        O.mc_reference_rng(op, 932117, 1, 2000)
+        one = 2000 / (time.perf_counter() - t)
+        per = int(max(2000, min(200000, one * args.cpu_seconds)))
+        t = time.perf_counter()
+        _, _, _ = O.mc_reference_rng(op, 932117, threads, per)
+        dt = time.perf_counter() - t
+        base = {"value": threads * per / dt, "unit": "electrons/s", "cores": threads,
+                "kind": "port",
+                "sample": f"{threads} streams x {per} electrons, the reference's generator and "
+                          f"OpenMP layout (private 1501^2 x {nE} histograms), binary64 "
+                          f"restatement of CTEMMC.f90:307-529",
+                "single_thread_electrons_per_s": one}
+    line = {
+        "metric": "Monte-Carlo electrons/s (CTEMMC defaults: Ni, 30 keV, 1501^2 x 41 bins)",
+        "value": value, "unit": "electrons/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "f64",
+        "data": "synthetic (material numbers of Ni)",
+        "config": {"workload": "ctemmc-ni-30kev-1501", "electrons_per_step": N,
+                   "backscatter_fraction": counted / (N * args.steps)},
+        "e2e": {"value": e2e, "unit": "electrons/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(he.nbytes + hz.nbytes), "steps": e2e_steps},
+        "gpu_launches": 1 * args.steps, "clocks": ck, "cpu_baseline": base}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = _args()
     if args.impl == "reference":
@@ -650,6 +735,8 @@ def main():
         return run_batched(args)
     if args.workload == "c5":
         return run_gn(args)
+    if args.workload == "mc":
+        return run_mc(args)
     return run_ours(args)
 
 

@@ -268,14 +268,23 @@ int64_t oracle_mc_philox(const oracle_mc_params* p, uint64_t seed, int64_t e0, i
 }
 
 /* The reference's own streams: for i = 1..nthreads, rng_seed(primeseed+i),
- * then num_el electrons in sequence (CTEMMC.f90:224-237). */
+ * then num_el electrons in sequence (CTEMMC.f90:224-237).  As in the
+ * reference, each stream runs on its own OpenMP thread into private
+ * histograms that are added at the end (the CRITICAL section of :234-237);
+ * integer sums, so the result does not depend on the thread count. */
 int64_t oracle_mc_reference_rng(const oracle_mc_params* p, int32_t primeseed, int nthreads,
                                 int64_t num_el, int32_t* accum_e, int32_t* accum_z)
 {
     mcs_t s;
     if (setup(p, &s)) return -1;
+    const size_t ne = (size_t)s.numEbins * s.numsx * s.numsx;
+    const size_t w10 = 2 * (size_t)s.nz10 + 1;
+    const size_t nzs = (size_t)s.numEbins * s.numzbins * w10 * w10;
     int64_t n = 0;
+#pragma omp parallel for schedule(static, 1) reduction(+ : n)
     for (int i = 1; i <= nthreads; ++i) {
+        int32_t* ae = (int32_t*)calloc(ne, sizeof(int32_t));
+        int32_t* az = accum_z ? (int32_t*)calloc(nzs, sizeof(int32_t)) : NULL;
         rng_t r;
         memset(&r, 0, sizeof r);
         r.kind = 1;
@@ -283,7 +292,19 @@ int64_t oracle_mc_reference_rng(const oracle_mc_params* p, int32_t primeseed, in
         r.st[1] = 362436069;
         r.st[2] = 16163801;
         r.st[3] = 1131199299;
-        for (int64_t e = 0; e < num_el; ++e) n += electron(&s, &r, accum_e, accum_z);
+        int64_t c = 0;
+        if (ae && (az || !accum_z))
+            for (int64_t e = 0; e < num_el; ++e) c += electron(&s, &r, ae, az);
+#pragma omp critical
+        {
+            if (ae)
+                for (size_t k = 0; k < ne; ++k) accum_e[k] += ae[k];
+            if (az)
+                for (size_t k = 0; k < nzs; ++k) accum_z[k] += az[k];
+        }
+        free(ae);
+        free(az);
+        n += c;
     }
     return n;
 }

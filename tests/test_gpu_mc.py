@@ -91,12 +91,14 @@ def test_statistics_against_the_reference_generator(built):
     assert chi2 < 3 * m.sum(), chi2
 
 
-def test_ctemmc_program_feeds_the_pattern_loop(built, tmp_path):
+def test_ctemmc_program_feeds_the_pattern_loop(built, tmp_path, monkeypatch):
+    # dataname is character(60) in the reference: a relative name in the run folder
+    monkeypatch.chdir(tmp_path)
     (tmp_path / "mc.nml").write_text(
         "&MCdata xtalname = 'Ni.xtal', density = 8.908, Ze = 28.0, at_wt = 58.6934,\n"
         " sig = 70.0, numsx = 121, num_el = 50000, nthreads = 2, primeseed = 5,\n"
         " EkeV = 20.0, Ehistmin = 16.0, Ebinsize = 1.0, depthmax = 100.0, depthstep = 1.0,\n"
-        f" dataname = '{tmp_path / 'MC.data'}' /\n")
+        " dataname = 'MC.data' /\n")
     capi.run_mc_namelist(tmp_path / "mc.nml")
     hdr, acc = capi.read_mc_file(tmp_path / "MC.data")
     assert (hdr.numEbins, hdr.numsx, hdr.numsy, hdr.num_el_total, hdr.nthreads) == (5, 121, 121,

@@ -36,6 +36,9 @@ def test_mc_namelist_keys(lib, tmp_path):
     assert n["xtalname"] == "Ni.xtal" and n["sig"] == 75.0 and n["numsx"] == 501
     assert n["num_el"] == 3000000000 and n["EkeV"] == 25.0 and n["Ehistmin"] == 15.0
     assert n["dataname"] == "out.data" and n["density"] == 8.9 and n["Ze"] == 28.0
+    # dataname is character(60) in the reference (CTEMMC.f90:135)
+    p.write_text("&MCdata dataname = '" + "d" * 70 + "' /\n")
+    assert capi.read_mc_namelist(p)["dataname"] == "d" * 60
     p.write_text("&MCdata bogus = 1 /\n")
     with pytest.raises(capi.EBSDError) as e:
         capi.read_mc_namelist(p)
