@@ -427,6 +427,11 @@ extern "C" int ebsd_set_master(ebsd_handle* h, const float* sr, int32_t npx, int
     if (nE > 4 * kMaxNV)
         return set_err(h, EBSD_EUNSUPPORTED, "ebsd_set_master: nE=%d exceeds %d energy bins", nE,
                        4 * kMaxNV);
+    // the pattern kernels address master nodes with 32-bit offsets
+    if ((double)(2 * npx + 1) * (double)(2 * npy + 1) * kMaxNV >= 2147483648.0)
+        return set_err(h, EBSD_EUNSUPPORTED,
+                       "ebsd_set_master: a %dx%d grid exceeds the 2^31 float4 node offsets",
+                       2 * npx + 1, 2 * npy + 1);
     int rc = activate(h);
     if (rc) return rc;
     const size_t n = (size_t)(2 * npx + 1) * (2 * npy + 1) * nE * numset;

@@ -13,7 +13,8 @@
 // Arithmetic follows the reference operation by operation (the TU is
 // compiled with -fmad=false, IEEE div/sqrt): the summation order of :600-604,
 // the binary64 prefactor multiply of :608, the column-major block sums of
-// :636 and powf for 'gam'.  Only atanf and powf are CUDA's own.
+// :636 and powf for 'gam' (the hardware __powf outside the reference-order
+// variant).  Only atanf and the power function are CUDA's own.
 #include "ebsd_device.cuh"
 #include "ebsd_internal.h"
 #include "ebsd_noise.cuh"
@@ -24,17 +25,15 @@ namespace {
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
-// 'gam' scaling, pattern**gammavalue (CTEMEBSD.f90:647-649).  A build-time
-// switch selects the hardware exp2/log2 form (__powf) for positive values.
-#ifndef EBSD_FAST_GAMMA
-#define EBSD_FAST_GAMMA 0
-#endif
-#ifndef EBSD_ADDR32
-#define EBSD_ADDR32 0
-#endif
+// 'gam' scaling, pattern**gammavalue (CTEMEBSD.f90:647-649).  The
+// reference-order variant (STRICT) calls powf; the default takes the
+// hardware exp2/log2 form (__powf, a few ulps) for positive values, 6 % of
+// the kernel's time at 640x480 against parity gates of 1e-5 (FP64) and
+// 1e-4 (reference).
+template <bool STRICT>
 __device__ __forceinline__ float gamma_pow(float x, float g)
 {
-    if (EBSD_FAST_GAMMA && x > 0.0f) return __powf(x, g);
+    if (!STRICT && x > 0.0f) return __powf(x, g);
     return powf(x, g);
 }
 
@@ -51,18 +50,12 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
                                               float dy, const float4 (&w)[NV], uint64_t pol)
 {
     const float dxm = 1.0f - dx, dym = 1.0f - dy;
-#if EBSD_ADDR32
-    // node offsets in 32 bits (the interleaved master holds < 2^31 float4)
+    // node offsets in 32 bits: ebsd_set_master keeps the interleaved master
+    // below 2^31 float4
     const float4* m00 = master + (uint32_t)(iy0 * gx + ix0) * (uint32_t)NV;
     const float4* m10 = master + (uint32_t)(iy0 * gx + ix1) * (uint32_t)NV;
     const float4* m01 = master + (uint32_t)(iy1 * gx + ix0) * (uint32_t)NV;
     const float4* m11 = master + (uint32_t)(iy1 * gx + ix1) * (uint32_t)NV;
-#else
-    const float4* m00 = master + ((int64_t)iy0 * gx + ix0) * NV;
-    const float4* m10 = master + ((int64_t)iy0 * gx + ix1) * NV;
-    const float4* m01 = master + ((int64_t)iy1 * gx + ix0) * NV;
-    const float4* m11 = master + ((int64_t)iy1 * gx + ix1) * NV;
-#endif
     if (STRICT) {
         float acc = 0.0f;
 #pragma unroll
@@ -152,7 +145,7 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
             }
         }
         if (!binned) {
-            if (prm.mode == EBSD_SCALING_GAM) val = gamma_pow(val, prm.gammavalue);  // :647-649
+            if (prm.mode == EBSD_SCALING_GAM) val = gamma_pow<STRICT>(val, prm.gammavalue);
             if (inside) __stcs(prm.out + o * rec + p, val);
         } else {
             const int b = prm.binning;
@@ -164,7 +157,7 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
                 for (int jj = 0; jj < b; ++jj)
                     for (int ii = 0; ii < b; ++ii) s = s + tile[(ty * b + jj) * 33 + tx * b + ii];
                 s = s * prm.bindx;                                           // :640
-                if (prm.mode == EBSD_SCALING_GAM) s = gamma_pow(s, prm.gammavalue);
+                if (prm.mode == EBSD_SCALING_GAM) s = gamma_pow<STRICT>(s, prm.gammavalue);
                 const int X = ((t % tiles_x) * kTileX) / b + tx;
                 const int Y = ((t / tiles_x) * tile_y) / b + ty;
                 if (X < prm.out_nx && Y < prm.out_ny)

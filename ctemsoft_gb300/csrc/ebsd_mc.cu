@@ -27,12 +27,6 @@ namespace ebsd {
 
 namespace {
 
-// A build-time switch for cheaper binary64 forms (sqrt for sin(acos), sincospi,
-// an integer-to-float uniform map), statistically equivalent only.
-#ifndef EBSD_MC_FAST
-#define EBSD_MC_FAST 0
-#endif
-
 constexpr double kPresig = 1.5273987e19, kScaled = 1.0e8, kMinEnergy = 1.0;
 constexpr int kMaxSteps = 5000;  // CTEMMC.f90:431
 
@@ -62,12 +56,8 @@ struct Stream {
         }
         const uint32_t w = pos == 0 ? b0 : pos == 1 ? b1 : pos == 2 ? b2 : b3;
         ++pos;
-#if EBSD_MC_FAST
-        return (double)(((float)(w >> 8) + 0.5f) * (1.0f / 16777216.0f));
-#else
         // rng.f95: u = real(0.5d0 + 0.23283064d-9 * imz), a single-precision value
         return (double)(float)(0.5 + 0.23283064e-9 * (double)(int32_t)w);
-#endif
     }
 };
 
@@ -161,16 +151,10 @@ __global__ void __launch_bounds__(256) k_mc(const McConsts K, uint64_t seed, lon
         }
         const double r1 = rng.next();
         const double cphi = 1.0 - 2.0 * alpha * r1 / (1.0 + alpha - r1);
-#if EBSD_MC_FAST
-        const double sphi = sqrt((1.0 - cphi) * (1.0 + cphi));
-        double spsi, cpsi;
-        sincospi(2.0 * rng.next(), &spsi, &cpsi);
-#else
         const double sphi = sin(acos(cphi));
         const double psi = K.tpi * rng.next();
         double spsi, cpsi;
         sincos(psi, &spsi, &cpsi);
-#endif
         double cp[3];
         if (fabs(cxyz[2]) > 0.99999) {
             cp[0] = sphi * cpsi;

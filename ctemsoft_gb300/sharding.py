@@ -97,3 +97,37 @@ def allreduce_sum(arrays, group=None):
         out.append(flat[i:i + a.size].reshape(a.shape))
         i += a.size
     return out
+
+
+def allreduce_sum_int(arrays, group=None):
+    """Exact sum of integer numpy arrays across torch.distributed ranks (int64
+    on the wire); identity when not initialised."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [np.asarray(a) for a in arrays]
+    flat = np.concatenate([np.asarray(a, np.int64).ravel() for a in arrays])
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
+    t = torch.from_numpy(flat).to(dev)
+    dist.all_reduce(t, group=group)
+    flat = t.cpu().numpy()
+    out, i = [], 0
+    for a in arrays:
+        a = np.asarray(a)
+        out.append(flat[i:i + a.size].reshape(a.shape).astype(a.dtype))
+        i += a.size
+    return out
+
+
+def mc_sharded(run, n_total: int, rank: int = 0, world: int = 1, group=None):
+    """Monte-Carlo histograms of electrons [0, n_total) spread over ranks:
+    this rank runs its contiguous range with run(first, n) -> (accum_e,
+    accum_z, counted) -- e.g. a Handle.mc_run bound to the parameters and
+    seed -- and the integer histograms are summed across ranks.  Each
+    electron's random stream depends only on (seed, electron index), so the
+    result equals a one-GPU run of all n_total electrons."""
+    b, e = shard_range(n_total, rank, world)
+    acc, accz, counted = run(b, e - b)
+    arrays = [acc, np.array([counted], np.int64)] + ([accz] if accz is not None else [])
+    summed = allreduce_sum_int(arrays, group)
+    return summed[0], (summed[2] if accz is not None else None), int(summed[1][0])

@@ -155,17 +155,53 @@ def test_vjp_rejects_gamma(built):
 
 
 def test_adjoint_480x480_npx500(built):
-    """The adjoint configuration: 480x480 detector, 1001^2 x 11 master."""
+    """The adjoint configuration: 480x480 detector, 1001^2 x 11 master, targets
+    simulated at orientations perturbed by N(0, 0.5 deg) and pattern centres
+    perturbed by N(0, 2 px) in xpc/ypc and N(0, 50 um) in L; loss 1 - normalised
+    dot product; FP32 adjoint against the FP64 analytic gradient and central
+    FP64 finite differences (h = 1e-4 rad, 1e-3 px, 1e-2 um)."""
     from oracle import oracle as O
     wl = synth.C4
     sr, acc = workload_data(wl)
     q = wl.quaternions(6)
     h, pref = _handle(wl, sr, acc)
-    T = _targets(O, wl, sr, acc, q, 1)
+    rng = np.random.default_rng(3)
+    geom = dict(wl.geometry(), exact=True)
+    T = []
+    for x in q.astype(np.float64):
+        gt = dict(geom)
+        gt["xpc"] += rng.normal(0, 2.0)
+        gt["ypc"] += rng.normal(0, 2.0)
+        gt["L"] += rng.normal(0, 50.0)
+        qt = O.rotate_left(x, np.radians(rng.normal(0, 0.5, 3)))
+        T.append(O.Detector(gt, acc, 1, wl.nEbins).patterns_f64(sr, qt[None], 1.0)[0])
+    T = np.stack(T).astype(np.float32)
     loss, g = h.vjp(q, capi.epilogue(pref), T, "ndp")
     rloss, rg = O.vjp_f64(wl.geometry(), acc, 1, wl.nEbins, sr, q, pref, 1, "ndp", T)
     np.testing.assert_allclose(loss, rloss, rtol=1e-3)
     err = _grad_err(g, rg)
-    print("480x480 grad rel err:", err)
+    print("480x480 grad rel err vs FP64 analytic (rot, xpc, ypc, L):", err)
     assert (err < TOL_GRAD).all(), err
+
+    def L(gm, qs):
+        P = O.Detector(gm, acc, 1, wl.nEbins).patterns_f64(sr, qs, 1.0,
+                                                            nthreads=O.max_threads())
+        return np.array([1 - (a * t).sum() / np.sqrt((a * a).sum() * (t * t).sum())
+                         for a, t in zip(P, T.astype(np.float64))])
+
+    qd = q.astype(np.float64)
+    fd = np.zeros((len(q), 6))
+    for a in range(3):
+        w = np.zeros(3)
+        w[a] = 1e-4
+        fd[:, a] = (L(geom, np.stack([O.rotate_left(x, w) for x in qd])) -
+                    L(geom, np.stack([O.rotate_left(x, -w) for x in qd]))) / 2e-4
+    for a, (k, st) in enumerate((("xpc", 1e-3), ("ypc", 1e-3), ("L", 1e-2))):
+        gp, gm = dict(geom), dict(geom)
+        gp[k] += st
+        gm[k] -= st
+        fd[:, 3 + a] = (L(gp, qd) - L(gm, qd)) / (2 * st)
+    err = _grad_err(g, fd)
+    print("480x480 grad rel err vs FP64 central differences:", err)
+    assert (err < TOL_FD).all(), err
     h.close()

@@ -113,3 +113,37 @@ def test_gloo_two_ranks_shared_centre():
     res = dict(q.get(timeout=5) for _ in range(2))
     assert max(res.values()) < 1e-12
     del torch
+
+
+def _mc_worker(rank, world, port, q):
+    import torch.distributed as dist
+    from oracle import oracle as O
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        p = O.mc_params(numsx=61)
+
+        def run(first, n):
+            return O.mc_philox(p, 13, first, first + n)
+
+        acc, accz, n = sharding.mc_sharded(run, 3001, rank, world)
+        ref, refz, nref = O.mc_philox(p, 13, 0, 3001)
+        q.put((rank, bool(np.array_equal(acc, ref) and np.array_equal(accz, refz) and n == nref)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_gloo_two_ranks_monte_carlo_ranges_sum_to_one_run():
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_mc_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+    assert all(p.exitcode == 0 for p in procs)
+    res = dict(q.get(timeout=5) for _ in range(2))
+    assert all(res.values())
