@@ -52,7 +52,7 @@ def _args():
     ap.add_argument("--vjp-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "mc"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "mc", "dict"],
                     help="c2: 640x480 plain forward (default); c3: 64-job batch; "
                          "c5: Gauss-Newton refinement")
     ap.add_argument("--c3-jobs", type=int, default=64,
@@ -62,6 +62,8 @@ def _args():
     ap.add_argument("--gn-orient", type=int, default=100000)
     ap.add_argument("--mc-electrons", type=int, default=20000000,
                     help="mc: electrons per timed step")
+    ap.add_argument("--dict-steps", type=int, default=100,
+                    help="dict: cubochoric steps per semi-edge of the m-3m zone")
     ap.add_argument("--fd-iters", type=int, default=3)
     return ap.parse_args()
 
@@ -727,6 +729,67 @@ def run_mc(args):
     return 0
 
 
+def run_dictionary(args):
+    """A dictionary: the m-3m fundamental zone sampled on the cubochoric grid
+    (ebsd_sample_rfz, N steps per semi-edge) straight into the pattern loop
+    on the 640x480 detector of the production workload, binned 8x8 to 80x60
+    records with gamma 0.33, everything on the device.  One step = sampling
+    + all patterns."""
+    import torch
+
+    from ctemsoft_gb300 import capi
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    wl, sr, acc, _ = _setup_data(0, 1)
+    h = capi.Handle(0)
+    h.set_master(sr)
+    num_el = h.set_detector(wl.geometry(), acc, 1, wl.nEbins)
+    epi = capi.epilogue(capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el), binning=8,
+                        scalingmode="gam", gammavalue=0.33)
+    nx, ny = h.output_dims(epi)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    h.set_stream(stream.cuda_stream)
+    import ctypes as C
+    cnt = C.c_int64()
+    N = args.dict_steps
+    capi._check(capi.lib().ebsd_sample_rfz(h.raw, N, 32, None, None, 0, C.byref(cnt)), h.raw)
+    n = cnt.value
+    dq = torch.empty((n, 4), device=dev)
+    out = torch.empty((n, ny, nx), device=dev)
+
+    def step():
+        capi._check(capi.lib().ebsd_sample_rfz(h.raw, N, 32, None, capi._ptr(dq), n,
+                                               C.byref(cnt)), h.raw)
+        h.forward(dq, epi, out=out)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.steps):
+        step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    ms = a.elapsed_time(b) / args.steps
+    t0 = time.perf_counter()
+    h.sample_rfz(N, 32)
+    samp_ms = (time.perf_counter() - t0) * 1e3
+    line = {
+        "metric": "dictionary patterns/s (m-3m zone, 640x480 binned 8 -> 80x60)",
+        "value": n / (ms / 1e3), "unit": "patterns/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": f"dictionary-m3m-N{N}-640x480-bin8",
+                                         "orientations": n, "grid_points": (2 * N + 1) ** 3},
+        "sampling_ms_host_call": samp_ms, "clocks": ck, "gpu_launches": 5 * args.steps}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = _args()
     if args.impl == "reference":
@@ -737,6 +800,8 @@ def main():
         return run_gn(args)
     if args.workload == "mc":
         return run_mc(args)
+    if args.workload == "dict":
+        return run_dictionary(args)
     return run_ours(args)
 
 

@@ -86,6 +86,7 @@ struct ebsd_handle {
     int max_persist = 0, max_window = 0;
 
     LaunchCfg cfg;
+    int mc_fp32 = 0;     // Monte-Carlo trajectories in binary32
     int vjp_tile_y = 4;  // adjoint / Gauss-Newton CTA height (8 for binning 8)
     int vjp_opc = 8;     // adjoint / Gauss-Newton orientations per CTA
     int weights_fp64 = 1;
@@ -402,6 +403,8 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
         if (value < 1 || value > 64)
             return set_err(h, EBSD_EINVAL, "orient_per_cta must be in 1..64");
         h->cfg.orient_per_cta = (int)value;
+    } else if (k == "mc_fp32") {
+        h->mc_fp32 = value != 0;
     } else if (k == "vjp_tile_y") {
         if (value != 4 && value != 8)
             return set_err(h, EBSD_EINVAL, "vjp_tile_y must be 4 or 8");
@@ -1726,7 +1729,8 @@ extern "C" int ebsd_mc_run(ebsd_handle* h, const ebsd_mc_params* p, uint64_t see
     CK(h, cudaMemsetAsync(de, 0, ne * 4, s), "histogram clear");
     if (dz) CK(h, cudaMemsetAsync(dz, 0, nzs * 4, s), "histogram clear");
     CK(h, cudaMemsetAsync(dcnt, 0, sizeof(unsigned long long), s), "counter clear");
-    CK(h, launch_mc(K, seed, first_electron, n_electrons, de, dz, dcnt, s), "Monte-Carlo kernel");
+    CK(h, launch_mc(K, seed, first_electron, n_electrons, de, dz, dcnt, h->mc_fp32 != 0, s),
+       "Monte-Carlo kernel");
     unsigned long long c = 0;
     CK(h, cudaMemcpyAsync(&c, dcnt, sizeof c, cudaMemcpyDeviceToHost, s), "counter copy");
     if (!edev) CK(h, cudaMemcpyAsync(accum_e, de, ne * 4, cudaMemcpyDeviceToHost, s), "accum_e copy");

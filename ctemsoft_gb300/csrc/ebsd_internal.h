@@ -172,6 +172,6 @@ struct McConsts {
 McConsts mc_constants(const ebsd_mc_params& p);
 cudaError_t launch_mc(const McConsts& K, uint64_t seed, long long e0, long long n,
                       int32_t* accum_e, int32_t* accum_z, unsigned long long* counted,
-                      cudaStream_t s);
+                      bool fp32, cudaStream_t s);
 
 }  // namespace ebsd

@@ -17,6 +17,7 @@
 // whose electron finishes starts its next one on the next iteration, so a
 // warp stays inside the step body instead of waiting for its longest
 // trajectory.  Counts are added with integer atomics.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -61,30 +62,80 @@ struct Stream {
     }
 };
 
-__device__ __forceinline__ void free_path(const McConsts& K, double Ec, double& alpha,
-                                          double& lambda)
+// Arithmetic of one precision: binary64 (the reference's, the default) or
+// binary32 (option mc_fp32: the same steps in single precision; the float
+// Lambert inverse takes the single-precision norm tolerance of
+// Lambert.f90:405-436).
+template <typename T>
+struct Math;
+template <>
+struct Math<double> {
+    static constexpr double kNormEps = 1.0e-12;
+    __device__ static double log_(double x) { return log(x); }
+    __device__ static double sin_(double x) { return sin(x); }
+    __device__ static double acos_(double x) { return acos(x); }
+    __device__ static double sqrt_(double x) { return sqrt(x); }
+    __device__ static double atan_(double x) { return atan(x); }
+    __device__ static void sincos_(double x, double* s, double* c) { sincos(x, s, c); }
+    __device__ static long long round_(double x) { return llround(x); }
+};
+template <>
+struct Math<float> {
+    static constexpr float kNormEps = 1.0e-6f;
+    __device__ static float log_(float x) { return logf(x); }
+    __device__ static float sin_(float x) { return sinf(x); }
+    __device__ static float acos_(float x) { return acosf(x); }
+    __device__ static float sqrt_(float x) { return sqrtf(x); }
+    __device__ static float atan_(float x) { return atanf(x); }
+    __device__ static void sincos_(float x, float* s, float* c) { sincosf(x, s, c); }
+    __device__ static long long round_(float x) { return llroundf(x); }
+};
+
+// McConsts in the working precision.
+template <typename T>
+struct Kc {
+    T EkeV, Ehistmin, Ebinsize, depthstep, Ze, Emin, pre, prealpha, J, predEds, tpi, tano, delta,
+        sPi2, cxstart, czstart, presig, scaled, min_energy;
+    int nx, nz10, numEbins, numzbins;
+    __device__ explicit Kc(const McConsts& K)
+        : EkeV((T)K.EkeV), Ehistmin((T)K.Ehistmin), Ebinsize((T)K.Ebinsize),
+          depthstep((T)K.depthstep), Ze((T)K.Ze), Emin((T)K.Emin), pre((T)K.pre),
+          prealpha((T)K.prealpha), J((T)K.J), predEds((T)K.predEds), tpi((T)K.tpi),
+          tano((T)K.tano), delta((T)K.delta), sPi2((T)K.sPi2), cxstart((T)K.cxstart),
+          czstart((T)K.czstart), presig((T)kPresig), scaled((T)kScaled),
+          min_energy((T)kMinEnergy), nx(K.nx), nz10(K.nz10), numEbins(K.numEbins),
+          numzbins(K.numzbins)
+    {
+    }
+};
+
+template <typename T>
+__device__ __forceinline__ void free_path(const Kc<T>& K, T Ec, T& alpha, T& lambda)
 {
     alpha = K.prealpha / Ec;
-    const double step = Ec * (Ec + 1024.0) / K.Ze / (Ec + 511.0);
-    const double sige = kPresig * step * step * alpha * (1.0 + alpha);
+    const T step = Ec * (Ec + (T)1024.0) / K.Ze / (Ec + (T)511.0);
+    const T sige = K.presig * step * step * alpha * ((T)1.0 + alpha);
     lambda = K.pre * sige;
 }
 
 // Record an exit (CTEMMC.f90:487-515); returns 1 if counted in accum_e.
-__device__ int record_exit(const McConsts& K, double Ec, const double xyz[3], const double cp[3],
+template <typename T>
+__device__ int record_exit(const Kc<T>& K, T Ec, const T xyz[3], const T cp[3],
                            int32_t* __restrict__ accum_e, int32_t* __restrict__ accum_z)
 {
-    // Lambert.f90:452-483, binary64 square-Lambert inverse, scaled
-    double X = 0.0, Y = 0.0;
-    const double n = cp[0] * cp[0] + cp[1] * cp[1] + cp[2] * cp[2];
-    if (!(fabs(1.0 - n) > 1.0e-12) && fabs(cp[2]) != 1.0) {
+    using F = Math<T>;
+    // Lambert.f90:452-483 (binary64) / :405-436 (binary32) square-Lambert
+    // inverse, scaled
+    T X = 0, Y = 0;
+    const T n = cp[0] * cp[0] + cp[1] * cp[1] + cp[2] * cp[2];
+    if (!(fabs((T)1.0 - n) > F::kNormEps) && fabs(cp[2]) != (T)1.0) {
         if (fabs(cp[1]) <= fabs(cp[0])) {
-            const double q = fabs(cp[0]) / cp[0] * sqrt(2.0 * (1.0 - cp[2]));
+            const T q = fabs(cp[0]) / cp[0] * F::sqrt_((T)2.0 * ((T)1.0 - cp[2]));
             X = q * K.sPi2;
-            Y = q * atan(cp[1] / cp[0]) / K.sPi2;
+            Y = q * F::atan_(cp[1] / cp[0]) / K.sPi2;
         } else {
-            const double q = fabs(cp[1]) / cp[1] * sqrt(2.0 * (1.0 - cp[2]));
-            X = q * atan(cp[0] / cp[1]) / K.sPi2;
+            const T q = fabs(cp[1]) / cp[1] * F::sqrt_((T)2.0 * ((T)1.0 - cp[2]));
+            X = q * F::atan_(cp[0] / cp[1]) / K.sPi2;
             Y = q * K.sPi2;
         }
     }
@@ -94,13 +145,13 @@ __device__ int record_exit(const McConsts& K, double Ec, const double xyz[3], co
     // rounding it would give an arbitrary index, so it is not counted
     if (!isfinite(X) || !isfinite(Y)) return 0;
     // nearest pixel with the frame reversal (x, y) -> (y, -x); nint = round half away
-    const long long ix = llround(Y), iy = llround(-X);
+    const long long ix = F::round_(Y), iy = F::round_(-X);
     if (llabs(ix) > K.nx || llabs(iy) > K.nx || !(Ec > K.Emin)) return 0;
-    const long long iE = llround((Ec - K.Ehistmin) / K.Ebinsize) + 1;
+    const long long iE = F::round_((Ec - K.Ehistmin) / K.Ebinsize) + 1;
     if (iE < 1 || iE > K.numEbins) return 0;  // the reference does not check
-    const double edis = fabs(xyz[2] / cp[2]);
-    const double zb = edis * 0.1 / K.depthstep;
-    const long long iz = zb < 1.0e15 ? llround(zb) + 1 : -1;  // inf/NaN: no depth bin
+    const T edis = fabs(xyz[2] / cp[2]);
+    const T zb = edis * (T)0.1 / K.depthstep;
+    const long long iz = zb < (T)1.0e15 ? F::round_(zb) + 1 : -1;  // inf/NaN: no depth bin
     if (iz > 0 && iz <= K.numzbins && accum_z) {
         const long long px = llroundf((float)ix / 10.0f), py = llroundf((float)iy / 10.0f);
         if (llabs(px) <= K.nz10 && llabs(py) <= K.nz10) {
@@ -116,17 +167,20 @@ __device__ int record_exit(const McConsts& K, double Ec, const double xyz[3], co
     return 1;
 }
 
-__global__ void __launch_bounds__(256) k_mc(const McConsts K, uint64_t seed, long long e0,
+template <typename T>
+__global__ void __launch_bounds__(256, 4) k_mc(const McConsts KD, uint64_t seed, long long e0,
                                             long long n, int32_t* __restrict__ accum_e,
                                             int32_t* __restrict__ accum_z,
                                             unsigned long long* __restrict__ counted)
 {
+    using F = Math<T>;
+    const Kc<T> K(KD);
     const long long stride = (long long)gridDim.x * blockDim.x;
     long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long mine = 0;
     Stream rng;
-    double Ec = 0.0, alpha = 0.0, lambda = 0.0, step = 0.0;
-    double xyz[3], cxyz[3];
+    T Ec = 0, alpha = 0, lambda = 0, step = 0;
+    T xyz[3], cxyz[3];
     int traj = kMaxSteps;  // "no electron in flight"
     for (;;) {
         if (traj >= kMaxSteps) {  // start the next electron (CTEMMC.f90:444-466)
@@ -135,44 +189,44 @@ __global__ void __launch_bounds__(256) k_mc(const McConsts K, uint64_t seed, lon
             k += stride;
             Ec = K.EkeV;
             free_path(K, Ec, alpha, lambda);
-            step = -lambda * log(rng.next());
+            step = -lambda * F::log_((T)rng.next());
             cxyz[0] = K.cxstart;
-            cxyz[1] = 0.0;
+            cxyz[1] = 0;
             cxyz[2] = K.czstart;
-            for (int i = 0; i < 3; ++i) xyz[i] = 0.0 + step * kScaled * cxyz[i];
+            for (int i = 0; i < 3; ++i) xyz[i] = (T)0.0 + step * K.scaled * cxyz[i];
             traj = 0;
         }
         // one scattering step (CTEMMC.f90:469-521)
-        const double dEds = K.predEds * log(Ec * K.J + 1.0) / Ec;
+        const T dEds = K.predEds * F::log_(Ec * K.J + (T)1.0) / Ec;
         Ec = Ec + dEds * step;
-        if (Ec < kMinEnergy) {
+        if (Ec < K.min_energy) {
             traj = kMaxSteps;
             continue;
         }
-        const double r1 = rng.next();
-        const double cphi = 1.0 - 2.0 * alpha * r1 / (1.0 + alpha - r1);
-        const double sphi = sin(acos(cphi));
-        const double psi = K.tpi * rng.next();
-        double spsi, cpsi;
-        sincos(psi, &spsi, &cpsi);
-        double cp[3];
-        if (fabs(cxyz[2]) > 0.99999) {
+        const T r1 = (T)rng.next();
+        const T cphi = (T)1.0 - (T)2.0 * alpha * r1 / ((T)1.0 + alpha - r1);
+        const T sphi = F::sin_(F::acos_(cphi));
+        const T psi = K.tpi * (T)rng.next();
+        T spsi, cpsi;
+        F::sincos_(psi, &spsi, &cpsi);
+        T cp[3];
+        if (fabs(cxyz[2]) > (T)0.99999) {
             cp[0] = sphi * cpsi;
             cp[1] = sphi * spsi;
             cp[2] = (cxyz[2] / fabs(cxyz[2])) * cphi;
         } else {
-            const double dsq = sqrt(1.0 - cxyz[2] * cxyz[2]);
-            const double dsqi = 1.0 / dsq;
+            const T dsq = F::sqrt_((T)1.0 - cxyz[2] * cxyz[2]);
+            const T dsqi = (T)1.0 / dsq;
             cp[0] = sphi * (cxyz[0] * cxyz[2] * cpsi - cxyz[1] * spsi) * dsqi + cxyz[0] * cphi;
             cp[1] = sphi * (cxyz[1] * cxyz[2] * cpsi + cxyz[0] * spsi) * dsqi + cxyz[1] * cphi;
             cp[2] = -(sphi * cpsi * dsq) + cxyz[2] * cphi;
         }
-        const double dd = 1.0 / sqrt(cp[0] * cp[0] + cp[1] * cp[1] + cp[2] * cp[2]);
+        const T dd = (T)1.0 / F::sqrt_(cp[0] * cp[0] + cp[1] * cp[1] + cp[2] * cp[2]);
         for (int i = 0; i < 3; ++i) cp[i] = cp[i] * dd;
         free_path(K, Ec, alpha, lambda);
-        step = -lambda * log(rng.next());
-        double xn[3];
-        for (int i = 0; i < 3; ++i) xn[i] = xyz[i] + step * kScaled * cp[i];
+        step = -lambda * F::log_((T)rng.next());
+        T xn[3];
+        for (int i = 0; i < 3; ++i) xn[i] = xyz[i] + step * K.scaled * cp[i];
         if (xn[2] > xn[1] * K.tano) {  // left the (double-tilted) surface
             mine += (unsigned long long)record_exit(K, Ec, xyz, cp, accum_e, accum_z);
             traj = kMaxSteps;
@@ -222,23 +276,29 @@ McConsts mc_constants(const ebsd_mc_params& p)
     return K;
 }
 
+template <typename T>
 int mc_grid()
 {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mc, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mc<T>, 256, 0);
     return sms * (per > 0 ? per : 1);
 }
 
 cudaError_t launch_mc(const McConsts& K, uint64_t seed, long long e0, long long n,
                       int32_t* accum_e, int32_t* accum_z, unsigned long long* counted,
-                      cudaStream_t s)
+                      bool fp32, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
     const long long want = (n + 255) / 256;
-    const int grid = (int)std::min<long long>(want, (long long)mc_grid());
-    k_mc<<<grid, 256, 0, s>>>(K, seed, e0, n, accum_e, accum_z, counted);
+    if (fp32) {
+        const int grid = (int)std::min<long long>(want, (long long)mc_grid<float>());
+        k_mc<float><<<grid, 256, 0, s>>>(K, seed, e0, n, accum_e, accum_z, counted);
+    } else {
+        const int grid = (int)std::min<long long>(want, (long long)mc_grid<double>());
+        k_mc<double><<<grid, 256, 0, s>>>(K, seed, e0, n, accum_e, accum_z, counted);
+    }
     return cudaGetLastError();
 }
 

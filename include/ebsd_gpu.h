@@ -100,7 +100,11 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    4 (default) or 8; binning 8 always uses 8.
  *   "vjp_orient_per_cta"  their orientations per CTA, 1..64 (default 8).
  *                    (ebsd_vjp_noalloc keeps 8 and 2, the shape its size
- *                    limit is stated for.) */
+ *                    limit is stated for.)
+ *   "mc_fp32"        0 (default): ebsd_mc_run in binary64, the reference's
+ *                    arithmetic; 1: the same trajectory steps in binary32,
+ *                    statistically equivalent (GB300's binary64 units bound
+ *                    the default's throughput). */
 int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value);
 
 /* Master pattern upload.  sr is the host array srtmp(-npx:npx,-npy:npy,nE,

@@ -120,3 +120,30 @@ def test_ctemmc_program_feeds_the_pattern_loop(built, tmp_path, monkeypatch):
     assert num_el > 0
     out = h.forward(wl.quaternions(4), capi.epilogue(capi.prefactor(15.0, 100.0, num_el)))
     assert np.isfinite(out).all() and out.max() > 0
+
+
+def test_fp32_option_is_statistically_equivalent(built):
+    """mc_fp32: the same trajectory steps in binary32.  On the same streams the
+    two precisions start from the same draws and drift apart only by
+    rounding, so backscatter fraction, energy spectrum and the coarse angular
+    distribution agree within counting noise."""
+    cp, _ = _pair()
+    h = capi.Handle(0)
+    a64, z64, n64 = h.mc_run(cp, 31, 0, 300000, accum_z=True)
+    h.set_option("mc_fp32", 1)
+    a32, z32, n32 = h.mc_run(cp, 31, 0, 300000, accum_z=True)
+    assert a32.sum() == n32 and abs(n32 - n64) < 4 * np.sqrt(n64)
+    e64, e32 = a64.sum(axis=(0, 1)).astype(float), a32.sum(axis=(0, 1)).astype(float)
+    m = (e64 + e32) > 20
+    chi2 = (((e64 - e32) ** 2) / (e64 + e32))[m].sum()
+    assert chi2 < 3 * m.sum(), chi2
+    # angular distribution on 10x10-pixel blocks
+    g64 = a64.sum(axis=2)[:100, :100].reshape(10, 10, 10, 10).sum(axis=(1, 3)).astype(float)
+    g32 = a32.sum(axis=2)[:100, :100].reshape(10, 10, 10, 10).sum(axis=(1, 3)).astype(float)
+    m = (g64 + g32) > 20
+    chi2 = (((g64 - g32) ** 2) / (g64 + g32))[m].sum()
+    assert chi2 < 3 * m.sum(), chi2
+    assert abs(int(z32.sum()) - int(z64.sum())) < 4 * np.sqrt(z64.sum())
+    h.set_option("mc_fp32", 0)
+    b64, _, m64 = h.mc_run(cp, 31, 0, 300000)
+    assert np.array_equal(b64, a64) and m64 == n64
