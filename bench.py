@@ -50,6 +50,7 @@ def _args():
     ap.add_argument("--orient", type=int, default=10000)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--vjp-steps", type=int, default=3)
+    ap.add_argument("--noise-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "mc", "dict"],
@@ -281,6 +282,28 @@ def run_ours(args):
     if args.vjp_steps > 0:
         fwd_vjp = _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, value)
 
+    # the same loop with the reference's Poisson noise (CTEMEBSD.f90:611-615)
+    # before the gamma epilogue
+    fwd_noise = None
+    if args.noise_steps > 0:
+        epn = capi.epilogue(pref, binning=1, scalingmode="gam", gammavalue=wl.gammavalue,
+                            poisson=True, seed=7)
+        h.forward(dq, epn, out=dout)
+        barrier()
+        evn = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.noise_steps)]
+        for k in range(args.noise_steps):
+            flush.zero_()
+            evn[k][0].record(stream)
+            h.forward(dq, epn, out=dout)
+            evn[k][1].record(stream)
+        barrier()
+        nms = sum(a.elapsed_time(b) for a, b in evn) / args.noise_steps
+        fwd_noise = {"value": world * N / (nms / 1000.0), "unit": UNIT, "ms_per_step": nms,
+                     "steps": args.noise_steps,
+                     "what": "forward with Poisson noise (Philox4x32-10, inversion / PTRS) "
+                             "before gamma 0.33"}
+
     # end to end through the C ABI with host buffers
     del dout
     torch.cuda.empty_cache()
@@ -315,6 +338,7 @@ def run_ours(args):
                                  "L2-resident), so frac can exceed 1"},
             "e2e": e2e,
             "fwd_vjp": fwd_vjp,
+            "fwd_noise": fwd_noise,
             "gpu_launches": args.steps,
             "clocks": ck,
             "cpu_baseline": base,
@@ -687,6 +711,17 @@ def run_mc(args):
     ck = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
     value = N / (ms / 1e3)
+    # the binary32 option (statistically equivalent trajectories)
+    h.set_option("mc_fp32", 1)
+    h.mc_run(p, 999, 0, max(1, N // 10), accum_e=de, accum_z=dz)
+    a32, b32 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a32.record(stream)
+    _, _, c32 = h.mc_run(p, 932117, 0, N, accum_e=de, accum_z=dz)
+    b32.record(stream)
+    torch.cuda.synchronize()
+    fp32 = {"value": N / (a32.elapsed_time(b32) / 1e3), "unit": "electrons/s",
+            "backscatter_fraction": c32 / N, "option": "mc_fp32 = 1"}
+    h.set_option("mc_fp32", 0)
     # end to end: host histograms
     he = np.empty((1501, 1501, nE), np.int32)
     hz = np.empty((2 * n10 + 1, 2 * n10 + 1, nz, nE), np.int32)
@@ -724,7 +759,7 @@ def run_mc(args):
                    "backscatter_fraction": counted / (N * args.steps)},
         "e2e": {"value": e2e, "unit": "electrons/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(he.nbytes + hz.nbytes), "steps": e2e_steps},
-        "gpu_launches": 1 * args.steps, "clocks": ck, "cpu_baseline": base}
+        "fp32": fp32, "gpu_launches": 1 * args.steps, "clocks": ck, "cpu_baseline": base}
     print(json.dumps(line))
     return 0
 
@@ -747,6 +782,7 @@ def run_dictionary(args):
     epi = capi.epilogue(capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el), binning=8,
                         scalingmode="gam", gammavalue=0.33)
     nx, ny = h.output_dims(epi)
+    tuned = h.autotune(epi, 64, Path(tempfile.gettempdir()) / "ebsd_autotune.txt")
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     h.set_stream(stream.cuda_stream)
@@ -785,7 +821,9 @@ def run_dictionary(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
         "data": "synthetic", "config": {"workload": f"dictionary-m3m-N{N}-640x480-bin8",
                                          "orientations": n, "grid_points": (2 * N + 1) ** 3},
-        "sampling_ms_host_call": samp_ms, "clocks": ck, "gpu_launches": 5 * args.steps}
+        "sampling_ms_host_call": samp_ms, "launch_shape": {"tile_y": tuned[0],
+                                                            "orient_per_cta": tuned[1]},
+        "clocks": ck, "gpu_launches": 5 * args.steps}
     print(json.dumps(line))
     return 0
 

@@ -57,6 +57,31 @@ def test_batched_matches_per_job_launches(built):
         assert torch.equal(out, ref), f"job {i}"
 
 
+def test_batched_noise_jobs_match_per_job_launches(built):
+    """Jobs with Poisson noise run in their own launch groups; the noise is
+    keyed by (seed, pattern, pixel), so batched and per-job outputs agree
+    bit for bit."""
+    torch = pytest.importorskip("torch")
+    masters, jobs = _mixed_jobs(torch, seed=5)
+    noisy = []
+    for i, (h, q, epi, out) in enumerate(jobs):
+        if i % 2 == 0:
+            epi = capi.epilogue(epi.prefactor * 50.0, binning=epi.binning,
+                                scalingmode=epi.scalingmode, gammavalue=epi.gammavalue,
+                                poisson=True, seed=40 + i)
+        noisy.append((h, q, epi, out))
+    noisy[0][0].forward_batched(noisy, graph=True)
+    torch.cuda.synchronize()
+    for i, (h, q, epi, out) in enumerate(noisy):
+        ref = torch.empty_like(out)
+        h.forward(q, epi, out=ref)
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref), f"job {i}"
+        if i % 2 == 0 and epi.scalingmode == capi.SCALING["not"]:
+            v = out.cpu().numpy()
+            assert np.array_equal(v, np.round(v))  # counts
+
+
 def test_batched_graph_replays_new_inputs(built):
     torch = pytest.importorskip("torch")
     masters, jobs = _mixed_jobs(torch)
