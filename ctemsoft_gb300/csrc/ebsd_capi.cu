@@ -87,6 +87,7 @@ struct ebsd_handle {
 
     LaunchCfg cfg;
     int mc_fp32 = 0;     // Monte-Carlo trajectories in binary32
+    int host_direct = 0; // kernel stores straight into pinned host outputs
     int vjp_tile_y = 4;  // adjoint / Gauss-Newton CTA height (8 for binning 8)
     int vjp_opc = 8;     // adjoint / Gauss-Newton orientations per CTA
     int weights_fp64 = 1;
@@ -405,6 +406,8 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
         h->cfg.orient_per_cta = (int)value;
     } else if (k == "mc_fp32") {
         h->mc_fp32 = value != 0;
+    } else if (k == "host_direct") {
+        h->host_direct = value != 0;
     } else if (k == "vjp_tile_y") {
         if (value != 4 && value != 8)
             return set_err(h, EBSD_EINVAL, "vjp_tile_y must be 4 or 8");
@@ -699,6 +702,32 @@ extern "C" int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const
             dq = (const float4*)h->quats[0].ptr;
         }
         return launch_chunk(h, p, dq, n, out);
+    }
+
+    // Pinned host output with host_direct: the kernel stores the records
+    // straight into the caller's buffer through its mapped device address
+    // (over NVLink-C2C on Grace systems), no staging copy.
+    // (the last byte must be pinned too: a kernel store past a mapped region
+    // would fault the GPU, where a copy only fails)
+    const float* last = out + (size_t)n * rec - 1;
+    if (ok == kPinned && h->host_direct && ptr_kind(last) == kPinned) {
+        void* dout = nullptr;
+        if (cudaHostGetDevicePointer(&dout, out, 0) == cudaSuccess && dout) {
+            const float4* dq = (const float4*)quats;
+            if (qk != kDevice) {
+                rc = ensure(h, h->quats[0], sizeof(float4) * (size_t)n, "quaternions");
+                if (rc) return rc;
+                CK(h, cudaMemcpyAsync(h->quats[0].ptr, quats, sizeof(float4) * n,
+                                      cudaMemcpyHostToDevice, s),
+                   "quaternion upload");
+                dq = (const float4*)h->quats[0].ptr;
+            }
+            rc = launch_chunk(h, p, dq, n, (float*)dout);
+            if (rc) return rc;
+            CK(h, cudaStreamSynchronize(s), "forward");
+            return EBSD_OK;
+        }
+        cudaGetLastError();  // not mapped: take the copy path below
     }
 
     // Host output: chunks of orientations, computed on the work stream and

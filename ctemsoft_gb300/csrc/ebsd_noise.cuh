@@ -78,6 +78,38 @@ struct PixelRng {
     }
 };
 
+// log k! for k = 0..15 (ln of the factorials).
+__device__ __constant__ float c_log_fact[16] = {
+    0.000000000e+00f, 0.000000000e+00f, 6.931471806e-01f, 1.791759469e+00f,
+    3.178053830e+00f, 4.787491743e+00f, 6.579251212e+00f, 8.525161361e+00f,
+    1.060460290e+01f, 1.280182748e+01f, 1.510441257e+01f, 1.750230785e+01f,
+    1.998721450e+01f, 2.255216385e+01f, 2.519122118e+01f, 2.789927138e+01f};
+
+// log of the Poisson probability p(k; lambda) = exp(-lambda) lambda^k / k!,
+// without the cancellation of the direct form (whose terms grow like
+// lambda log lambda).  For k >= 16, Stirling's series
+//   log k! = k log k - k + log(2 pi k)/2 + 1/(12k) - 1/(360k^3) + ...
+// gives log p = -lambda h(x) - log(2 pi k)/2 - 1/(12k) + 1/(360k^3),
+// x = (k - lambda)/lambda, h(x) = (1+x) log(1+x) - x, summed as its power
+// series sum_{n>=2} (-x)^n / (n (n-1)) (times -1 for odd n) near 0.
+__device__ __forceinline__ float log_poisson_pmf(float k, float lambda, float loglam)
+{
+    if (k < 16.0f) return -lambda + k * loglam - c_log_fact[(int)k];
+    const float x = (k - lambda) / lambda;
+    float h;
+    if (fabsf(x) < 0.125f) {
+        // x^2/2 - x^3/6 + x^4/12 - x^5/20 + x^6/30 - x^7/42 + x^8/56
+        const float x2 = x * x;
+        h = x2 * (0.5f + x * (-1.0f / 6.0f + x * (1.0f / 12.0f + x * (-1.0f / 20.0f +
+             x * (1.0f / 30.0f + x * (-1.0f / 42.0f + x * (1.0f / 56.0f)))))));
+    } else {
+        h = (1.0f + x) * log1pf(x) - x;
+    }
+    const float ik = 1.0f / k;
+    return -lambda * h - 0.5f * logf(6.28318531f * k) - ik * (1.0f / 12.0f) +
+           ik * ik * ik * (1.0f / 360.0f);
+}
+
 // One Poisson(lambda) draw.  lambda <= 0 (or NaN) gives 0.
 __device__ __forceinline__ float poisson_draw(float lambda, PixelRng& rng)
 {
@@ -98,7 +130,7 @@ __device__ __forceinline__ float poisson_draw(float lambda, PixelRng& rng)
     const float slam = sqrtf(lambda), loglam = logf(lambda);
     const float b = 0.931f + 2.53f * slam;
     const float a = -0.059f + 0.02483f * b;
-    const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
+    const float loginvalpha = logf(1.1239f + 1.1328f / (b - 3.4f));
     const float vr = 0.9277f - 3.6224f / (b - 2.0f);
     for (int it = 0; it < 64; ++it) {  // acceptance > 0.85 per try
         const float U = rng.next() - 0.5f;
@@ -107,8 +139,7 @@ __device__ __forceinline__ float poisson_draw(float lambda, PixelRng& rng)
         const float k = floorf((2.0f * a / us + b) * U + lambda + 0.43f);
         if (us >= 0.07f && V <= vr) return k;
         if (k < 0.0f || (us < 0.013f && V > us)) continue;
-        if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <=
-            -lambda + k * loglam - lgammaf(k + 1.0f))
+        if (logf(V) + loginvalpha - logf(a / (us * us) + b) <= log_poisson_pmf(k, lambda, loglam))
             return k;
     }
     return floorf(lambda + 0.5f);  // not reached in practice (p < 1e-50)

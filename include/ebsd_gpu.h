@@ -101,6 +101,10 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *   "vjp_orient_per_cta"  their orientations per CTA, 1..64 (default 8).
  *                    (ebsd_vjp_noalloc keeps 8 and 2, the shape its size
  *                    limit is stated for.)
+ *   "host_direct"    0 (default): patterns for a host destination are
+ *                    computed into device chunks and copied back; 1: for a
+ *                    pinned destination the pattern kernel stores the records
+ *                    straight into it through its mapped address.
  *   "mc_fp32"        0 (default): ebsd_mc_run in binary64, the reference's
  *                    arithmetic; 1: the same trajectory steps in binary32,
  *                    statistically equivalent and, since GB300's binary64

@@ -307,3 +307,27 @@ def test_misaligned_device_quaternions_are_refused(built):
     good[:, 0] = 1.0
     assert L.ebsd_forward(h.raw, good.data_ptr(), 3, C.byref(epi), capi._ptr(out)) == 0
     h.close()
+
+
+def test_host_direct_matches_the_copy_path(built):
+    """Option host_direct: the kernel stores into the pinned destination
+    directly; the records are identical to the staged-copy path."""
+    torch = pytest.importorskip("torch")
+    wl = synth.tiny(seed=9, numsx=64, numsy=48, npx=60, nE=5, mc_nsx=80, n_orient=37)
+    h, det, sr, num_el = _setup(wl)
+    epi = capi.epilogue(capi.prefactor(15.0, 100.0, num_el), binning=2, scalingmode="gam",
+                        gammavalue=0.33)
+    q = wl.quaternions()
+    ox, oy = h.output_dims(epi)
+    hq = torch.from_numpy(q).pin_memory()
+    a = torch.full((len(q), oy, ox), -1.0).pin_memory()
+    b = torch.full((len(q), oy, ox), -2.0).pin_memory()
+    h.forward(hq, epi, out=a)
+    h.set_option("host_direct", 1)
+    h.forward(hq, epi, out=b)
+    assert torch.equal(a, b)
+    dq = torch.from_numpy(q).cuda()
+    c = torch.full((len(q), oy, ox), -3.0).pin_memory()
+    h.forward(dq, epi, out=c)  # device quaternions, pinned output
+    assert torch.equal(a, c)
+    h.close()

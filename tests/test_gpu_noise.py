@@ -19,7 +19,7 @@ def _setup():
     return wl, h
 
 
-@pytest.mark.parametrize("target_mean", [3.0, 1000.0])
+@pytest.mark.parametrize("target_mean", [3.0, 1000.0, 1.0e5])
 def test_poisson_moments(built, target_mean):
     wl, h = _setup()
     q1 = wl.quaternions(1)
@@ -70,3 +70,36 @@ def test_poisson_reproducible_and_chunk_independent(built):
                                        poisson=True, seed=9))
     ref = (a[:5].reshape(5, 6, 4, 8, 4).sum(axis=(2, 4)) / 16.0) ** 0.5
     np.testing.assert_allclose(g, ref, rtol=2e-6)
+
+
+@pytest.mark.parametrize("lam", [12.5, 340.0, 2.0e4, 1.0e6])
+def test_poisson_distribution_shape(built, lam):
+    """The whole distribution, not only its moments: a uniform master with
+    uniform weights gives every pixel the same mean, and 1.2 M draws are
+    binned by standardised value and checked against the exact Poisson pmf
+    (chi-square over bins with expected count >= 20)."""
+    from scipy import stats
+    wl = synth.tiny(numsx=64, numsy=48, npx=40, nE=5)
+    sr = np.ones_like(wl.master())
+    h = capi.Handle(0)
+    h.set_master(sr)
+    h.set_detector(wl.geometry(), wl.mc(), 1, 5)
+    q = wl.quaternions(1)
+    clean = h.forward(q, capi.epilogue(1.0))[0].astype(np.float64)
+    inner = clean[8:-8, 8:-8]
+    pref = lam / inner.mean()
+    qq = np.repeat(q, 400, axis=0)
+    noisy = h.forward(qq, capi.epilogue(pref, poisson=True, seed=77))[:, 8:-8, 8:-8]
+    lams = (inner * pref)[None].repeat(400, 0)
+    # per-pixel means differ slightly (MC weights): compare each draw's
+    # Poisson CDF value, which is uniform for the exact distribution
+    k = noisy.astype(np.float64).ravel()
+    lv = lams.ravel()
+    u_lo = stats.poisson.cdf(k - 1, lv)
+    u_hi = stats.poisson.cdf(k, lv)
+    rng = np.random.default_rng(1)
+    u = u_lo + (u_hi - u_lo) * rng.random(u_lo.size)   # randomised PIT
+    hist, _ = np.histogram(u, bins=50, range=(0, 1))
+    exp = u.size / 50
+    chi2 = ((hist - exp) ** 2 / exp).sum()
+    assert chi2 < 100, chi2  # 49 degrees of freedom
