@@ -87,7 +87,7 @@ struct ebsd_handle {
 
     LaunchCfg cfg;
     int mc_fp32 = 0;     // Monte-Carlo trajectories in binary32
-    int host_direct = 0; // kernel stores straight into pinned host outputs
+    int host_direct = 1; // kernel stores straight into pinned host outputs
     int vjp_tile_y = 4;  // adjoint / Gauss-Newton CTA height (8 for binning 8)
     int vjp_opc = 8;     // adjoint / Gauss-Newton orientations per CTA
     int weights_fp64 = 1;

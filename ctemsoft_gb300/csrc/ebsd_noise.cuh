@@ -92,10 +92,16 @@ __device__ __constant__ float c_log_fact[16] = {
 // gives log p = -lambda h(x) - log(2 pi k)/2 - 1/(12k) + 1/(360k^3),
 // x = (k - lambda)/lambda, h(x) = (1+x) log(1+x) - x, summed as its power
 // series sum_{n>=2} (-x)^n / (n (n-1)) (times -1 for odd n) near 0.
+//
+// The sampler only needs statistical accuracy: logarithms, exponentials and
+// divides use the hardware intrinsics (__logf, __expf, __fdividef; errors of
+// order 1e-6, far below what changes a distribution).  The pattern means sit
+// around 10 at the reference's beam settings, so most warps run both the
+// inversion and the PTRS branch and the cost of each shows.
 __device__ __forceinline__ float log_poisson_pmf(float k, float lambda, float loglam)
 {
     if (k < 16.0f) return -lambda + k * loglam - c_log_fact[(int)k];
-    const float x = (k - lambda) / lambda;
+    const float x = __fdividef(k - lambda, lambda);
     float h;
     if (fabsf(x) < 0.125f) {
         // x^2/2 - x^3/6 + x^4/12 - x^5/20 + x^6/30 - x^7/42 + x^8/56
@@ -103,10 +109,10 @@ __device__ __forceinline__ float log_poisson_pmf(float k, float lambda, float lo
         h = x2 * (0.5f + x * (-1.0f / 6.0f + x * (1.0f / 12.0f + x * (-1.0f / 20.0f +
              x * (1.0f / 30.0f + x * (-1.0f / 42.0f + x * (1.0f / 56.0f)))))));
     } else {
-        h = (1.0f + x) * log1pf(x) - x;
+        h = (1.0f + x) * __logf(1.0f + x) - x;
     }
-    const float ik = 1.0f / k;
-    return -lambda * h - 0.5f * logf(6.28318531f * k) - ik * (1.0f / 12.0f) +
+    const float ik = __fdividef(1.0f, k);
+    return -lambda * h - 0.5f * __logf(6.28318531f * k) - ik * (1.0f / 12.0f) +
            ik * ik * ik * (1.0f / 360.0f);
 }
 
@@ -117,29 +123,30 @@ __device__ __forceinline__ float poisson_draw(float lambda, PixelRng& rng)
     if (lambda < 10.0f) {
         // inversion: walk the cumulative distribution from k = 0
         const float u = rng.next();
-        float p = expf(-lambda), cdf = p;
+        float p = __expf(-lambda), cdf = p;
         int k = 0;
         while (u > cdf && k < 200) {
             ++k;
-            p *= lambda / (float)k;
+            p *= __fdividef(lambda, (float)k);
             cdf += p;
         }
         return (float)k;
     }
     // PTRS, Hormann (1993), constants from the paper
-    const float slam = sqrtf(lambda), loglam = logf(lambda);
+    const float slam = sqrtf(lambda), loglam = __logf(lambda);
     const float b = 0.931f + 2.53f * slam;
     const float a = -0.059f + 0.02483f * b;
-    const float loginvalpha = logf(1.1239f + 1.1328f / (b - 3.4f));
-    const float vr = 0.9277f - 3.6224f / (b - 2.0f);
+    const float loginvalpha = __logf(1.1239f + __fdividef(1.1328f, b - 3.4f));
+    const float vr = 0.9277f - __fdividef(3.6224f, b - 2.0f);
     for (int it = 0; it < 64; ++it) {  // acceptance > 0.85 per try
         const float U = rng.next() - 0.5f;
         const float V = rng.next();
         const float us = 0.5f - fabsf(U);
-        const float k = floorf((2.0f * a / us + b) * U + lambda + 0.43f);
+        const float k = floorf((__fdividef(2.0f * a, us) + b) * U + lambda + 0.43f);
         if (us >= 0.07f && V <= vr) return k;
         if (k < 0.0f || (us < 0.013f && V > us)) continue;
-        if (logf(V) + loginvalpha - logf(a / (us * us) + b) <= log_poisson_pmf(k, lambda, loglam))
+        if (__logf(V) + loginvalpha - __logf(__fdividef(a, us * us) + b) <=
+            log_poisson_pmf(k, lambda, loglam))
             return k;
     }
     return floorf(lambda + 0.5f);  // not reached in practice (p < 1e-50)

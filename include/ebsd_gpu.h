@@ -101,10 +101,12 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *   "vjp_orient_per_cta"  their orientations per CTA, 1..64 (default 8).
  *                    (ebsd_vjp_noalloc keeps 8 and 2, the shape its size
  *                    limit is stated for.)
- *   "host_direct"    0 (default): patterns for a host destination are
- *                    computed into device chunks and copied back; 1: for a
- *                    pinned destination the pattern kernel stores the records
- *                    straight into it through its mapped address.
+ *   "host_direct"    1 (default): for a pinned host destination the pattern
+ *                    kernel stores the records straight into it through its
+ *                    mapped address (157 k patterns/s end to end at 640x480
+ *                    on GB300, where device chunks + copies gave 87-154 k);
+ *                    0: device chunks copied back on a second stream (always
+ *                    the path for pageable destinations).
  *   "mc_fp32"        0 (default): ebsd_mc_run in binary64, the reference's
  *                    arithmetic; 1: the same trajectory steps in binary32,
  *                    statistically equivalent and, since GB300's binary64

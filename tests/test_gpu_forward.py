@@ -322,6 +322,7 @@ def test_host_direct_matches_the_copy_path(built):
     hq = torch.from_numpy(q).pin_memory()
     a = torch.full((len(q), oy, ox), -1.0).pin_memory()
     b = torch.full((len(q), oy, ox), -2.0).pin_memory()
+    h.set_option("host_direct", 0)
     h.forward(hq, epi, out=a)
     h.set_option("host_direct", 1)
     h.forward(hq, epi, out=b)

@@ -75,7 +75,7 @@ def test_poisson_reproducible_and_chunk_independent(built):
 @pytest.mark.parametrize("lam", [12.5, 340.0, 2.0e4, 1.0e6])
 def test_poisson_distribution_shape(built, lam):
     """The whole distribution, not only its moments: a uniform master with
-    uniform weights gives every pixel the same mean, and 1.2 M draws are
+    uniform weights gives every pixel nearly the same mean, and 614 k draws are
     binned by standardised value and checked against the exact Poisson pmf
     (chi-square over bins with expected count >= 20)."""
     from scipy import stats
