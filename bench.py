@@ -237,6 +237,9 @@ def run_ours(args):
     epi = capi.epilogue(pref, binning=1, scalingmode="gam", gammavalue=wl.gammavalue)
     nx, ny = h.output_dims(epi)
     P = wl.numsx * wl.numsy
+    # the launch shape from the project's autotuner (cached per shape), as a
+    # caller would run it; tuning happens before and outside the timed steps
+    tuned = h.autotune(epi, 256, Path(tempfile.gettempdir()) / f"ebsd_autotune_{local}.txt")
 
     # a dedicated stream: its handle is never 0, which the C ABI reads as
     # "the handle's own stream"; the events below are recorded on it
@@ -329,7 +332,9 @@ def run_ours(args):
                        "master": f"{2 * wl.npx + 1}^2 x {wl.nEbins} bins",
                        "orientations_per_gpu": N, "epilogue": "prefactor, gamma 0.33",
                        "l2": "flushed (512 MB write) between timed steps",
-                       "parallelism": f"orientation shards x{world}"},
+                       "parallelism": f"orientation shards x{world}",
+                       "launch_shape": {"tile_y": tuned[0], "orient_per_cta": tuned[1],
+                                        "source": "ebsd_autotune"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": (tpp * N if tpp else None),
