@@ -302,8 +302,21 @@ def run_ours(args):
             evn[k][1].record(stream)
         barrier()
         nms = sum(a.elapsed_time(b) for a, b in evn) / args.noise_steps
+        # the sampler's branches: means ~1 (inversion), ~10 (the reference's
+        # beam settings: both), ~100 (PTRS), one step each
+        by_mean = {}
+        for scale in (0.1, 1.0, 10.0):
+            eps = capi.epilogue(pref * scale, binning=1, scalingmode="gam",
+                                gammavalue=wl.gammavalue, poisson=True, seed=8)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            flush.zero_()
+            a.record(stream)
+            h.forward(dq, eps, out=dout)
+            b.record(stream)
+            torch.cuda.synchronize()
+            by_mean[f"prefactor x{scale:g}"] = N / (a.elapsed_time(b) / 1000.0)
         fwd_noise = {"value": world * N / (nms / 1000.0), "unit": UNIT, "ms_per_step": nms,
-                     "steps": args.noise_steps,
+                     "steps": args.noise_steps, "by_prefactor_scale": by_mean,
                      "what": "forward with Poisson noise (Philox4x32-10, inversion / PTRS) "
                              "before gamma 0.33"}
 

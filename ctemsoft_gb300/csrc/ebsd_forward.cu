@@ -168,8 +168,17 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
     }
 }
 
+// Launch bounds: CTAs of up to 512 threads (tile_y 16).  A build may trade
+// the largest tile for a register budget with more resident CTAs
+// (EBSD_FWD_MAX_THREADS and EBSD_FWD_MIN_BLOCKS).
+#ifdef EBSD_FWD_MIN_BLOCKS
+#define EBSD_FWD_LAUNCH_BOUNDS __launch_bounds__(EBSD_FWD_MAX_THREADS, EBSD_FWD_MIN_BLOCKS)
+#else
+#define EBSD_FWD_LAUNCH_BOUNDS __launch_bounds__(512)
+#endif
+
 template <int NV, bool STRICT, bool NOISE>
-__global__ void __launch_bounds__(512) k_forward(const FwdParams prm, int tile_y, int tiles_x,
+__global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y, int tiles_x,
                                                  int ntiles, int opc)
 {
     extern __shared__ float tile[];  // [tile_y][33], binning only
