@@ -271,7 +271,11 @@ __global__ void k_cells(const FwdParams prm)
 template <int NV, bool STRICT, bool NOISE>
 cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
-    const int tile_y = cfg.tile_y;
+    // binned records are summed inside a CTA: its height must hold whole
+    // b x b blocks (binning 8 on a 4-row tile would write nothing)
+    int tile_y = cfg.tile_y;
+    if (p.mode != EBSD_SCALING_NOT && p.binning > 1)
+        while (tile_y % p.binning != 0 && tile_y < 16) tile_y *= 2;
     const int tiles_x = (p.numsx + kTileX - 1) / kTileX;
     const int tiles_y = (p.numsy + tile_y - 1) / tile_y;
     const int ntiles = tiles_x * tiles_y;

@@ -80,8 +80,8 @@ struct BatchHeader {
 
 // Launch configuration picked by the tuner or by default.
 struct LaunchCfg {
-    int tile_y = 8;        // CTA is 32 x tile_y pixels
-    int orient_per_cta = 4;
+    int tile_y = 4;        // CTA is 32 x tile_y pixels (raised to 8 for binning 8)
+    int orient_per_cta = 8;
     bool strict = false;   // reference summation order in the gather
     // L2 access-policy window kept persisting for the master pattern
     const void* persist_base = nullptr;

@@ -94,8 +94,9 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    rounded once; 0: the reference's single precision.
  *                    num_el (:516) always uses the reference's arithmetic.
  *                    Takes effect at the next ebsd_set_detector.
- *   "tile_y"         pattern-kernel CTA height in pixels: 4, 8 (default), 16.
- *   "orient_per_cta" orientations per CTA, 1..64 (default 4).
+ *   "tile_y"         pattern-kernel CTA height in pixels: 4 (default), 8, 16;
+ *                    raised to 8 when the epilogue bins 8x8.
+ *   "orient_per_cta" orientations per CTA, 1..64 (default 8).
  *   "vjp_tile_y"     CTA height of ebsd_vjp and the Gauss-Newton kernels:
  *                    4 (default) or 8; binning 8 always uses 8.
  *   "vjp_orient_per_cta"  their orientations per CTA, 1..64 (default 8).

@@ -332,3 +332,18 @@ def test_host_direct_matches_the_copy_path(built):
     h.forward(dq, epi, out=c)  # device quaternions, pinned output
     assert torch.equal(a, c)
     h.close()
+
+
+def test_binning_8_with_a_four_row_tile(built):
+    """A 4-row tile cannot hold an 8x8 block: the launch raises the tile height,
+    so the records equal those of an 8-row tile."""
+    wl = synth.tiny(seed=4, numsx=80, numsy=64, npx=60, nE=5, mc_nsx=80, n_orient=9)
+    h, det, sr, num_el = _setup(wl)
+    q = wl.quaternions()
+    epi = capi.epilogue(capi.prefactor(15.0, 100.0, num_el), binning=8, scalingmode="lin")
+    h.set_option("tile_y", 8)
+    a = h.forward(q, epi)
+    h.set_option("tile_y", 4)
+    b = h.forward(q, epi)
+    assert np.array_equal(a, b) and np.abs(a).max() > 0
+    h.close()
