@@ -33,16 +33,19 @@ __device__ __forceinline__ float4 ldg4_keep(const float4* p, uint64_t pol)
 }
 
 // qq3 = q (x) (0,r) (x) conjg(q), quaternions.f90:255-264,306-313 as used at
-// CTEMEBSD.f90:577-586; returns the vector part.
+// CTEMEBSD.f90:577-586; returns the vector part.  The first product's terms
+// with the zero scalar part of (0,r) are left out: 0*y is +-0 for finite y,
+// and (+-0) - a = -a, (+-0) + a = a exactly for every a != 0, so only the
+// sign of an exact-zero component can differ from the reference, which moves
+// neither a Lambert cell nor a value.
 __device__ __forceinline__ void rotate_direction(const float4 q, float rx, float ry, float rz,
                                                  float& d0, float& d1, float& d2)
 {
-    const float x0 = 0.0f;
     const float y0 = q.x, y1 = -q.y, y2 = -q.z, y3 = -q.w;   // conjg(q)
-    const float t0 = x0 * y0 - rx * y1 - ry * y2 - rz * y3;   // quat_mult(qq, qq1)
-    const float t1 = x0 * y1 + rx * y0 + ry * y3 - rz * y2;
-    const float t2 = x0 * y2 - rx * y3 + ry * y0 + rz * y1;
-    const float t3 = x0 * y3 + rx * y2 - ry * y1 + rz * y0;
+    const float t0 = -(rx * y1) - ry * y2 - rz * y3;           // quat_mult(qq, qq1)
+    const float t1 = rx * y0 + ry * y3 - rz * y2;
+    const float t2 = -(rx * y3) + ry * y0 + rz * y1;
+    const float t3 = rx * y2 - ry * y1 + rz * y0;
     d0 = q.x * t1 + q.y * t0 + q.z * t3 - q.w * t2;           // quat_mult(qq2, t)
     d1 = q.x * t2 - q.y * t3 + q.z * t0 + q.w * t1;
     d2 = q.x * t3 + q.y * t2 - q.z * t1 + q.w * t0;
