@@ -276,13 +276,15 @@ int check_quats_host(ebsd_handle* h, const float* q, int64_t n)
 }
 
 int launch_chunk(ebsd_handle* h, FwdParams p, const float4* dq, int64_t n, float* dout,
-                 int64_t o_offset = 0)
+                 int64_t o_offset = 0, bool host_out = false)
 {
     p.o_offset = o_offset;
     p.quats = dq;
     p.n = n;
     p.out = dout;
-    cudaError_t e = launch_forward(p, h->NV, h->cfg, h->stream);
+    LaunchCfg cfg = h->cfg;
+    if (host_out) cfg.warp_w = 32;  // whole 128-byte rows per warp store into host memory
+    cudaError_t e = launch_forward(p, h->NV, cfg, h->stream);
     if (e != cudaSuccess) return cuda_err(h, e, "forward kernel launch");
     return EBSD_OK;
 }
@@ -401,8 +403,8 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
             return set_err(h, EBSD_EINVAL, "tile_y must be 4, 8 or 16");
         h->cfg.tile_y = (int)value;
     } else if (k == "orient_per_cta") {
-        if (value < 1 || value > 64)
-            return set_err(h, EBSD_EINVAL, "orient_per_cta must be in 1..64");
+        if (value < 0 || value > 64)
+            return set_err(h, EBSD_EINVAL, "orient_per_cta must be in 0..64");
         h->cfg.orient_per_cta = (int)value;
     } else if (k == "mc_fp32") {
         h->mc_fp32 = value != 0;
@@ -722,7 +724,7 @@ extern "C" int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const
                    "quaternion upload");
                 dq = (const float4*)h->quats[0].ptr;
             }
-            rc = launch_chunk(h, p, dq, n, (float*)dout);
+            rc = launch_chunk(h, p, dq, n, (float*)dout, 0, true);
             if (rc) return rc;
             CK(h, cudaStreamSynchronize(s), "forward");
             return EBSD_OK;
@@ -1468,7 +1470,7 @@ extern "C" int ebsd_autotune(ebsd_handle* h, const ebsd_epilogue* e, int64_t n_s
         p.n = n_sample;
         best_us = INFINITY;
         const int tys[3] = {4, 8, 16};
-        const int opcs[4] = {1, 2, 4, 8};
+        const int opcs[7] = {1, 2, 4, 8, 16, 32, 64};
         for (int ty : tys) {
             if (ce != cudaSuccess) break;
             if (p.binning > 1 && p.mode != EBSD_SCALING_NOT && ty % p.binning != 0) continue;

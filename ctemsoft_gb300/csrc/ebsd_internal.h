@@ -15,7 +15,7 @@ namespace ebsd {
 constexpr int kMaxNV = 16;
 
 // Launch shapes the forward kernels accept.
-constexpr int kTileX = 32;  // pixels along x per CTA row (one warp)
+constexpr int kTileX = 32;  // pixels along x per CTA
 
 struct DeviceBuf {
     void* ptr = nullptr;
@@ -81,7 +81,8 @@ struct BatchHeader {
 // Launch configuration picked by the tuner or by default.
 struct LaunchCfg {
     int tile_y = 4;        // CTA is 32 x tile_y pixels (raised to 8 for binning 8)
-    int orient_per_cta = 8;
+    int orient_per_cta = 0;  // 0: chosen per launch from the grid size
+    int warp_w = 16;         // pixels along x per warp: 16 (16 x 2) or 32 (32 x 1)
     bool strict = false;   // reference summation order in the gather
     // L2 access-policy window kept persisting for the master pattern
     const void* persist_base = nullptr;

@@ -94,9 +94,23 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    rounded once; 0: the reference's single precision.
  *                    num_el (:516) always uses the reference's arithmetic.
  *                    Takes effect at the next ebsd_set_detector.
+ *   "strict_order"   0 (default): the pattern kernel sums the energy gather
+ *                    of CTEMEBSD.f90:600-604 as fused dot products and
+ *                    multiplies by the prefactor (:608) in binary32, each
+ *                    within a few ulps of the reference arithmetic; 1: the
+ *                    reference's summation order, unfused, and the binary64
+ *                    prefactor multiply.
+ *   "lambert_accurate" 0 (default): 1 - z as Lambert.f90:427,430 evaluate it;
+ *                    1: (x^2 + y^2) / (1 + z), free of the cancellation near
+ *                    the poles (cells may then differ from the reference's).
+ *   "l2_persist"     0 drops the persisting L2 window that ebsd_set_master
+ *                    places on the master (kept by default where the device
+ *                    offers one; 1 keeps it, an error if there is none).
  *   "tile_y"         pattern-kernel CTA height in pixels: 4 (default), 8, 16;
  *                    raised to 8 when the epilogue bins 8x8.
- *   "orient_per_cta" orientations per CTA, 1..64 (default 8).
+ *   "orient_per_cta" orientations per CTA, 1..64, or 0 (default): 64,
+ *                    halved while the launch would have fewer than 32 CTAs
+ *                    per SM.
  *   "vjp_tile_y"     CTA height of ebsd_vjp and the Gauss-Newton kernels:
  *                    4 (default) or 8; binning 8 always uses 8.
  *   "vjp_orient_per_cta"  their orientations per CTA, 1..64 (default 8).
