@@ -101,14 +101,17 @@ __device__ __forceinline__ void lambert_inverse(float x, float y, float z, float
     }
 }
 
-// lambert_inverse plus its Jacobian with respect to (x, y, z), sharing the
-// square root and arc tangent.  The point (X, Y) is computed by exactly the
-// operations of lambert_inverse, so cells agree with the forward kernels.
-// The Jacobian uses rho^2 = 2(x^2+y^2)/(1+z) (no cancellation at the poles)
-// and is zero where the map is intercepted (|z| = 1, non-unit input).
+// The square Lambert map of Lambert.f90:405-436 and its Jacobian with respect
+// to (x, y, z), for the adjoint kernels.  The adjoint does not need the
+// reference's rounding: the bilinear gather is continuous across cell edges,
+// so a point placed an ulp differently changes the value only by rounding.
+// So the map is evaluated in the cancellation-free form
+// rho^2 = 2(1 - z) = 2(x^2 + y^2)/(1 + z) with the hardware reciprocal
+// square root and fast divide (CUDA intrinsics, 2-ulp bounds) instead of the
+// IEEE operations of lambert_inverse.  Zero where the map is intercepted
+// (|z| = 1, non-unit input, or x = y = 0).
 __device__ __forceinline__ void lambert_inverse_jac(float x, float y, float z, float spi2,
-                                                    bool accurate, float& X, float& Y,
-                                                    float dX[3], float dY[3])
+                                                    float& X, float& Y, float dX[3], float dY[3])
 {
     float s = x * x;
     s = s + y * y;
@@ -116,28 +119,21 @@ __device__ __forceinline__ void lambert_inverse_jac(float x, float y, float z, f
     s = s + z * z;
     dX[0] = dX[1] = dX[2] = 0.0f;
     dY[0] = dY[1] = dY[2] = 0.0f;
-    if (fabsf(1.0f - s) > 1.0e-6f || fabsf(z) == 1.0f) {
-        X = 0.0f;
-        Y = 0.0f;
-        return;
-    }
-    const float omz = accurate ? rxy / (1.0f + z) : 1.0f - z;
+    X = 0.0f;
+    Y = 0.0f;
+    if (fabsf(1.0f - s) > 1.0e-6f || fabsf(z) == 1.0f || !(rxy > 0.0f)) return;
     const bool xb = fabsf(y) <= fabsf(x);
-    const float u = xb ? x : y, v = xb ? y : x;       // |v| <= |u|
-    const float q = copysignf(sqrtf(2.0f * omz), u);
-    const float a = atanf(v / u);
-    const float along = q * spi2, across = q * a / spi2;
-    X = xb ? along : across;
-    Y = xb ? across : along;
-    if (!(rxy > 0.0f)) return;
-    // The derivatives need relative accuracy, not the reference's rounding:
-    // the hardware reciprocal square root and fast divide (CUDA intrinsics,
-    // 2-ulp bounds) replace IEEE divisions here.
-    const float t = __fdividef(2.0f * rxy, 1.0f + z);
+    const float u = xb ? x : y, v = xb ? y : x;       // |v| <= |u|, u != 0
+    const float t = __fdividef(2.0f * rxy, 1.0f + z);  // rho^2 (z >= 0 after the fold)
     const float irho = rsqrtf(t);
     const float rho = t * irho;
     const float sg = copysignf(1.0f, u);
+    const float q = sg * rho;
+    const float a = atanf(__fdividef(v, u));
     const float ispi2 = __fdividef(1.0f, spi2);
+    const float along = q * spi2, across = q * a * ispi2;
+    X = xb ? along : across;
+    Y = xb ? across : along;
     const float f = sg * __fdividef(rho * ispi2, rxy);
     // d(along)/dz, d(across)/d(u, v, z)
     const float dal_z = -sg * spi2 * irho;

@@ -106,14 +106,20 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
                                              int64_t o_begin, int opc, float* tile, int bw)
 {
     const int tid = threadIdx.x;
+    const bool binned = prm.mode != EBSD_SCALING_NOT && prm.binning > 1;
+    const int b = prm.binning;
     // Each warp covers a bw x (32 / bw) block of the tile (bw = 16 or 32).
     // A 16 x 2 block of detector pixels gathers from a more compact patch of
     // the master than a 32 x 1 row, so a warp's loads touch fewer cache
     // lines (1-3 % faster at 640x480) while its stores stay whole 64-byte
-    // runs; stores into mapped host memory take whole 128-byte rows.
-    const int bh = 32 / bw, nbx = kTileX / bw;
+    // runs; stores into mapped host memory take whole 128-byte rows.  When
+    // the record is binned 2x2 or 4x4 the warp block holds whole binning
+    // blocks (16 x 2, 8 x 4), which are then summed within the warp.
+    if (binned && b == 4) bw = 8;
+    if (binned && b == 2 && bw > 16) bw = 16;
+    const int bh = 32 / bw, wpr = kTileX / bw;
     const int lane = tid & 31, wid = tid >> 5;
-    const int tx = (wid % nbx) * bw + lane % bw, ty = (wid / nbx) * bh + lane / bw;
+    const int tx = (wid % wpr) * bw + lane % bw, ty = (wid / wpr) * bh + lane / bw;
     const int x = (t % tiles_x) * kTileX + tx;
     const int y = (t / tiles_x) * tile_y + ty;
     const bool inside = x < prm.numsx && y < prm.numsy;
@@ -129,7 +135,6 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
 #pragma unroll
         for (int c = 0; c < NV; ++c) w[c] = ldg4_keep(prm.W + (int64_t)c * prm.P + p, pol);
     }
-    const bool binned = prm.mode != EBSD_SCALING_NOT && prm.binning > 1;
     const int64_t rec = (int64_t)prm.out_nx * prm.out_ny;
     const float pref32 = (float)prm.prefactor;
 
@@ -160,8 +165,22 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
         if (!binned) {
             if (prm.mode == EBSD_SCALING_GAM) val = gamma_pow<STRICT>(val, prm.gammavalue);
             if (inside) __stcs(prm.out + o * rec + p, val);
+        } else if (b <= 4) {
+            // the block's top-left lane adds its b x b pixels from their lanes
+            // in the order of the smem path below (:636), with no CTA barrier
+            float s = 0.0f;
+            for (int jj = 0; jj < b; ++jj)
+                for (int ii = 0; ii < b; ++ii)
+                    s = s + __shfl_sync(0xffffffffu, val, (lane + jj * bw + ii) & 31);
+            if (tx % b == 0 && ty % b == 0) {
+                s = s * prm.bindx;                                           // :640
+                if (prm.mode == EBSD_SCALING_GAM) s = gamma_pow<STRICT>(s, prm.gammavalue);
+                const int X = ((t % tiles_x) * kTileX + tx) / b;
+                const int Y = ((t / tiles_x) * tile_y + ty) / b;
+                if (X < prm.out_nx && Y < prm.out_ny)
+                    __stcs(prm.out + o * rec + (int64_t)Y * prm.out_nx + X, s);
+            }
         } else {
-            const int b = prm.binning;
             tile[ty * 33 + tx] = val;
             __syncthreads();
             const int nbx = kTileX / b, nby = tile_y / b;

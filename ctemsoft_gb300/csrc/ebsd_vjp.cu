@@ -58,14 +58,13 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     const float4 r = ldg4_keep(prm.rg + p, pol);
     float d0, d1, d2;
     rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
-    // derivative-only normalisation: hardware reciprocal square root
+    // normalisation and fold (:588-589) with the hardware reciprocal square
+    // root: the adjoint needs relative accuracy, not the reference's rounding
     const float ind = rsqrtf(fmaf(d0, d0, fmaf(d1, d1, d2 * d2)));
     const float h0 = d0 * ind, h1 = d1 * ind, h2 = d2 * ind;
-    float c0 = d0, c1 = d1, c2 = d2;
-    normalize_fold(c0, c1, c2);
     const float s = h2 < 0.0f ? -1.0f : 1.0f;
     float LX, LY, dX[3], dY[3];
-    lambert_inverse_jac(c0, c1, c2, prm.spi2, prm.accurate != 0, LX, LY, dX, dY);
+    lambert_inverse_jac(s * h0, s * h1, s * h2, prm.spi2, LX, LY, dX, dY);
     float dx, dy;
     int nix, niy;
     const int ix0 = lambert_cell(prm.scl * LX, prm.npx, dx, nix);
