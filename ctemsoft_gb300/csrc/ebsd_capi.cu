@@ -1213,6 +1213,18 @@ struct BatchGroup {
     std::vector<BatchJob> jobs;
 };
 
+// A job that fills the GPU by itself: launched on its own, at its handle's
+// (tuned) launch shape, inside the batch's stream or graph.
+struct BatchLarge {
+    FwdParams p;
+    int NV;
+    LaunchCfg cfg;
+};
+
+// A job whose own launch has at least this many CTAs per SM (several full
+// waves) runs as its own launch; smaller ones share the persistent queue.
+constexpr int kBatchLargeCtasPerSm = 64;
+
 }  // namespace
 
 extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_t njobs,
@@ -1223,7 +1235,10 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         return set_err(h, EBSD_EINVAL, "ebsd_forward_batched: bad job list");
     int rc = activate(h);
     if (rc) return rc;
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
     std::vector<BatchGroup> groups;
+    std::vector<BatchLarge> large;
     for (int j = 0; j < njobs; ++j) {
         const ebsd_job& J = jobs[j];
         ebsd_handle* src = J.source;
@@ -1248,6 +1263,15 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         b.p.quats = (const float4*)J.quats;
         b.p.out = J.out;
         b.p.n = J.n;
+        if (forward_ctas(b.p, src->cfg) >= (int64_t)kBatchLargeCtasPerSm * sms) {
+            BatchLarge L;
+            memset(&L, 0, sizeof L);
+            L.p = b.p;
+            L.NV = src->NV;
+            L.cfg = src->cfg;
+            large.push_back(L);
+            continue;
+        }
         const int ty = batch_tile_y(b.p.mode == EBSD_SCALING_NOT ? 1 : b.p.binning);
         b.tiles_x = (b.p.numsx + kTileX - 1) / kTileX;
         b.ntiles = b.tiles_x * ((b.p.numsy + ty - 1) / ty);
@@ -1267,7 +1291,7 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         }
         g->jobs.push_back(b);
     }
-    if (groups.empty()) return EBSD_OK;
+    if (groups.empty() && large.empty()) return EBSD_OK;
     std::sort(groups.begin(), groups.end(), [](const BatchGroup& a, const BatchGroup& b) {
         if (a.NV != b.NV) return a.NV < b.NV;
         if (a.noise != b.noise) return a.noise < b.noise;
@@ -1290,6 +1314,19 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         key.push_back(g.NV * 32 + (g.noise ? 16 : 0) + g.ty);
         key.push_back((int)g.jobs.size());
     }
+    // a large job's parameters are baked into the graph's kernel node: the
+    // graph is reused only for identical parameters (the same buffers)
+    for (auto& L : large) {
+        key.push_back(-1);
+        const int* w = reinterpret_cast<const int*>(&L.p);  // zero-filled padding
+        key.insert(key.end(), w, w + sizeof(FwdParams) / sizeof(int));
+        const uint64_t pb = (uint64_t)(uintptr_t)L.cfg.persist_base;
+        int hr;
+        memcpy(&hr, &L.cfg.persist_hit_ratio, sizeof hr);
+        key.insert(key.end(), {L.NV, L.cfg.tile_y, L.cfg.orient_per_cta, L.cfg.warp_w,
+                               (int)L.cfg.strict, (int)(pb >> 32), (int)pb,
+                               (int)(L.cfg.persist_bytes >> 32), (int)L.cfg.persist_bytes, hr});
+    }
     const bool use_graph = (flags & EBSD_BATCH_GRAPH) != 0;
     const bool reuse = use_graph && h->batch_exec && h->batch_key == key &&
                        h->batch_table_host_bytes >= bytes && h->batch_stream == h->stream;
@@ -1298,6 +1335,8 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
             cudaGraphExecDestroy(h->batch_exec);
             h->batch_exec = nullptr;
         }
+    }
+    if (!reuse && G > 0) {
         rc = ensure(h, h->batch_table, bytes, "batch table");
         if (rc) return rc;
         if (h->batch_table_host_bytes < bytes) {
@@ -1311,7 +1350,7 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
     // fill the pinned table
     char* ht = (char*)h->batch_table_host;
     char* dt = (char*)h->batch_table.ptr;
-    memset(ht, 0, bytes);
+    if (G > 0) memset(ht, 0, bytes);
     size_t jo = 0;
     std::vector<int> grids(G);
     for (size_t gi = 0; gi < G; ++gi) {
@@ -1336,7 +1375,11 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
     }
     cudaStream_t s = h->stream;
     auto enqueue = [&]() -> cudaError_t {
-        cudaError_t e = cudaMemcpyAsync(dt, ht, bytes, cudaMemcpyHostToDevice, s);
+        cudaError_t e = cudaSuccess;
+        for (size_t i = 0; i < large.size() && e == cudaSuccess; ++i)
+            e = launch_forward(large[i].p, large[i].NV, large[i].cfg, s);
+        if (G == 0) return e;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dt, ht, bytes, cudaMemcpyHostToDevice, s);
         if (e == cudaSuccess)
             e = cudaMemsetAsync(dt + cnt_off, 0, G * sizeof(unsigned long long), s);
         size_t j0 = 0;

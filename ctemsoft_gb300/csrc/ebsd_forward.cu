@@ -84,6 +84,31 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
     return fmaf(c00, dxm * dym, fmaf(c10, dx * dym, fmaf(c01, dxm * dy, c11 * (dx * dy))));
 }
 
+// Sum of the B x B binning block (B = 2 or 4) held by a warp of 32/B x B
+// lanes (lane = row * 32/B + column).  STRICT: each block's top-left lane
+// adds the B^2 values in the order of CTEMEBSD.f90:636 (x fastest).
+// Otherwise a butterfly over the block's columns, then its rows, leaves the
+// block total in every lane of the block.
+template <int B, bool STRICT>
+__device__ __forceinline__ float block_sum(float v, int lane)
+{
+    constexpr int BW = 32 / B;
+    if (STRICT) {
+        float s = 0.0f;
+#pragma unroll
+        for (int jj = 0; jj < B; ++jj)
+#pragma unroll
+            for (int ii = 0; ii < B; ++ii)
+                s = s + __shfl_sync(0xffffffffu, v, (lane + jj * BW + ii) & 31);
+        return s;
+    }
+#pragma unroll
+    for (int o = 1; o < B; o <<= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o);
+#pragma unroll
+    for (int o = 1; o < B; o <<= 1) v = v + __shfl_xor_sync(0xffffffffu, v, o * BW);
+    return v;
+}
+
 // Rotated, projected and scaled Lambert coordinates of one pixel for one
 // orientation (CTEMEBSD.f90:584-591).
 __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, float scl,
@@ -101,7 +126,10 @@ __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, fl
 
 // One work item: the 32 x tile_y pixels of tile t for orientations
 // [o_begin, o_begin + opc).  `tile` is shared scratch of tile_y x 33 floats.
-template <int NV, bool STRICT, bool NOISE>
+// BIN8: the variant for 8x8-binned records outside the reference-order mode
+// (its pair barriers are kept out of the other variants, where their
+// reservation would cost occupancy).
+template <int NV, bool STRICT, bool NOISE, bool BIN8 = false>
 __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, int tiles_x, int t,
                                              int64_t o_begin, int opc, float* tile, int bw)
 {
@@ -113,13 +141,21 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
     // the master than a 32 x 1 row, so a warp's loads touch fewer cache
     // lines (1-3 % faster at 640x480) while its stores stay whole 64-byte
     // runs; stores into mapped host memory take whole 128-byte rows.  When
-    // the record is binned 2x2 or 4x4 the warp block holds whole binning
+    // the record is binned 2x2 or 4x4 the warp block is one row of binning
     // blocks (16 x 2, 8 x 4), which are then summed within the warp.
-    if (binned && b == 4) bw = 8;
-    if (binned && b == 2 && bw > 16) bw = 16;
+    if (binned && b <= 4) bw = 32 / b;
+    if (BIN8) bw = 8;  // an 8x8 block is two 8 x 4 warps
     const int bh = 32 / bw, wpr = kTileX / bw;
     const int lane = tid & 31, wid = tid >> 5;
-    const int tx = (wid % wpr) * bw + lane % bw, ty = (wid / wpr) * bh + lane / bw;
+    int lx = lane % bw, ly = lane / bw;
+    if (!binned && bw == 16) {
+        // each quarter-warp (the lanes whose 128-bit loads the L1 serves
+        // together) a 4 x 2 block: its gathers span fewer cache lines than
+        // an 8 x 1 row (4 % faster at 640x480)
+        lx = (lane >> 3) * 4 + (lane & 3);
+        ly = (lane >> 2) & 1;
+    }
+    const int tx = (wid % wpr) * bw + lx, ty = (wid / wpr) * bh + ly;
     const int x = (t % tiles_x) * kTileX + tx;
     const int y = (t / tiles_x) * tile_y + ty;
     const bool inside = x < prm.numsx && y < prm.numsy;
@@ -166,19 +202,37 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
             if (prm.mode == EBSD_SCALING_GAM) val = gamma_pow<STRICT>(val, prm.gammavalue);
             if (inside) __stcs(prm.out + o * rec + p, val);
         } else if (b <= 4) {
-            // the block's top-left lane adds its b x b pixels from their lanes
-            // in the order of the smem path below (:636), with no CTA barrier
-            float s = 0.0f;
-            for (int jj = 0; jj < b; ++jj)
-                for (int ii = 0; ii < b; ++ii)
-                    s = s + __shfl_sync(0xffffffffu, val, (lane + jj * bw + ii) & 31);
-            if (tx % b == 0 && ty % b == 0) {
+            // whole blocks within the warp: no CTA barrier
+            float s = b == 2 ? block_sum<2, STRICT>(val, lane) : block_sum<4, STRICT>(val, lane);
+            if (lane < bw && (lane & (b - 1)) == 0) {                        // top-left lanes
                 s = s * prm.bindx;                                           // :640
                 if (prm.mode == EBSD_SCALING_GAM) s = gamma_pow<STRICT>(s, prm.gammavalue);
                 const int X = ((t % tiles_x) * kTileX + tx) / b;
                 const int Y = ((t / tiles_x) * tile_y + ty) / b;
                 if (X < prm.out_nx && Y < prm.out_ny)
                     __stcs(prm.out + o * rec + (int64_t)Y * prm.out_nx + X, s);
+            }
+        } else if (BIN8) {
+            // 8x8 blocks: each 8 x 4 warp sums its half by a butterfly; the
+            // lower warp hands its half to the upper one through shared
+            // memory (slots alternate with the orientation) and the pair
+            // meets at its own named barrier, not the CTA's
+            float sh = val;
+#pragma unroll
+            for (int m = 1; m < 32; m <<= 1) sh = sh + __shfl_xor_sync(0xffffffffu, sh, m);
+            const int rgrp = wid / wpr;                          // 4-row group of the tile
+            const int pair = (rgrp >> 1) * wpr + wid % wpr;      // 8x8 block within the tile
+            float* slot = tile + ((int)(o & 1) * 32 + pair);
+            if ((rgrp & 1) && lane == 0) *slot = sh;
+            asm volatile("bar.sync %0, 64;" ::"r"(1 + pair) : "memory");
+            if (!(rgrp & 1) && lane == 0) {
+                float sb = sh + *slot;
+                sb = sb * prm.bindx;                                         // :640
+                if (prm.mode == EBSD_SCALING_GAM) sb = gamma_pow<false>(sb, prm.gammavalue);
+                const int X = ((t % tiles_x) * kTileX) / 8 + wid % wpr;
+                const int Y = ((t / tiles_x) * tile_y) / 8 + (rgrp >> 1);
+                if (X < prm.out_nx && Y < prm.out_ny)
+                    __stcs(prm.out + o * rec + (int64_t)Y * prm.out_nx + X, sb);
             }
         } else {
             tile[ty * 33 + tx] = val;
@@ -231,14 +285,14 @@ int resolve_opc(int opc, int64_t n, int ntiles)
 #define EBSD_FWD_LAUNCH_BOUNDS __launch_bounds__(512)
 #endif
 
-template <int NV, bool STRICT, bool NOISE>
+template <int NV, bool STRICT, bool NOISE, bool BIN8>
 __global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y, int tiles_x,
                                                  int ntiles, int opc, int warp_w)
 {
     extern __shared__ float tile[];  // [tile_y][33], binning only
     const int t = (int)(blockIdx.x % (unsigned)ntiles);
     const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
-    forward_tile<NV, STRICT, NOISE>(prm, tile_y, tiles_x, t, o_begin, opc, tile, warp_w);
+    forward_tile<NV, STRICT, NOISE, BIN8>(prm, tile_y, tiles_x, t, o_begin, opc, tile, warp_w);
 }
 
 // Batched pattern loop: one persistent grid works through a queue of work
@@ -297,7 +351,8 @@ __global__ void __launch_bounds__(32 * TY, 32 / TY) k_forward_batched(const Batc
         const int64_t o_begin = s_obegin[slot];
         if (threadIdx.x == 0) claim(slot ^ 1);
         const BatchJob& J = jobs[job];
-        forward_tile<NV, false, NOISE>(J.p, TY, J.tiles_x, t, o_begin, J.opc, tile, 16);
+        // TY 8 groups hold the 8x8-binned jobs only
+        forward_tile<NV, false, NOISE, TY == 8>(J.p, TY, J.tiles_x, t, o_begin, J.opc, tile, 16);
         __syncthreads();
     }
 }
@@ -322,7 +377,7 @@ __global__ void k_cells(const FwdParams prm)
     prm.ixy1[idx] = ixy1;
 }
 
-template <int NV, bool STRICT, bool NOISE>
+template <int NV, bool STRICT, bool NOISE, bool BIN8 = false>
 cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
     // binned records are summed inside a CTA: its height must hold whole
@@ -345,16 +400,20 @@ cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
     cudaLaunchAttribute attr[1];
     set_persist_attr(cfg, attr, lc);
     const int warp_w = cfg.warp_w == 32 ? 32 : 16;
-    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE>, p, tile_y, tiles_x, ntiles, opc,
+    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE, BIN8>, p, tile_y, tiles_x, ntiles, opc,
                               warp_w);
 }
 
 template <int NV>
 cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
-    if (p.poisson) return launch_nv2<NV, false, true>(p, cfg, s);  // noise: fused gather
-    return cfg.strict ? launch_nv2<NV, true, false>(p, cfg, s)
-                      : launch_nv2<NV, false, false>(p, cfg, s);
+    const bool bin8 = !cfg.strict && p.mode != EBSD_SCALING_NOT && p.binning == 8;
+    if (p.poisson)  // noise: fused gather
+        return bin8 ? launch_nv2<NV, false, true, true>(p, cfg, s)
+                    : launch_nv2<NV, false, true>(p, cfg, s);
+    if (cfg.strict) return launch_nv2<NV, true, false>(p, cfg, s);
+    return bin8 ? launch_nv2<NV, false, false, true>(p, cfg, s)
+                : launch_nv2<NV, false, false>(p, cfg, s);
 }
 
 template <int NV, bool NOISE, int TY>
@@ -428,6 +487,16 @@ int batched_grid(int NV, bool noise, int ty)
         case 8: return batched_grid_nv<8>(noise, ty);
         default: return 0;
     }
+}
+
+int64_t forward_ctas(const FwdParams& p, const LaunchCfg& cfg)
+{
+    int tile_y = cfg.tile_y;
+    if (p.mode != EBSD_SCALING_NOT && p.binning > 1)
+        while (tile_y % p.binning != 0 && tile_y < 16) tile_y *= 2;
+    const int ntiles = ((p.numsx + kTileX - 1) / kTileX) * ((p.numsy + tile_y - 1) / tile_y);
+    const int opc = resolve_opc(cfg.orient_per_cta, p.n, ntiles);
+    return ((p.n + opc - 1) / opc) * (int64_t)ntiles;
 }
 
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s)

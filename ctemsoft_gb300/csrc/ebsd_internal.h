@@ -138,6 +138,8 @@ cudaError_t launch_gn_update(const double* sys, int64_t n, double lambda, const 
                              float4* quats, float* step, cudaStream_t s);
 
 // Pattern kernels (ebsd_forward.cu).
+// CTAs that launch_forward would start for p under cfg.
+int64_t forward_ctas(const FwdParams& p, const LaunchCfg& cfg);
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s);
 cudaError_t launch_cells(const FwdParams& p, int NV, cudaStream_t s);
 cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,

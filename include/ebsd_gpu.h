@@ -95,11 +95,12 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    num_el (:516) always uses the reference's arithmetic.
  *                    Takes effect at the next ebsd_set_detector.
  *   "strict_order"   0 (default): the pattern kernel sums the energy gather
- *                    of CTEMEBSD.f90:600-604 as fused dot products and
- *                    multiplies by the prefactor (:608) in binary32, each
- *                    within a few ulps of the reference arithmetic; 1: the
- *                    reference's summation order, unfused, and the binary64
- *                    prefactor multiply.
+ *                    of CTEMEBSD.f90:600-604 as fused dot products,
+ *                    multiplies by the prefactor (:608) in binary32 and sums
+ *                    binning blocks (:636) pairwise, each within a few ulps
+ *                    of the reference arithmetic; 1: the reference's
+ *                    summation orders, unfused, and the binary64 prefactor
+ *                    multiply.
  *   "lambert_accurate" 0 (default): 1 - z as Lambert.f90:427,430 evaluate it;
  *                    1: (x^2 + y^2) / (1 + z), free of the cancellation near
  *                    the poles (cells may then differ from the reference's).
@@ -183,7 +184,7 @@ typedef struct {
 
 /* Launch-shape autotuner (no reference counterpart): times the pattern
  * kernel for this handle's detector and epilogue over n_sample orientations
- * at 128, 256 and 512 pixels per CTA x 1, 2, 4 and 8 orientations per CTA,
+ * at 128, 256 and 512 pixels per CTA x 1 to 64 orientations per CTA,
  * applies the fastest, and appends it to cache_path (a text file of
  * "shape key|tile_y|orient_per_cta|us per pattern" lines; NULL = no file).
  * A shape already in the file is applied without timing.  Any of the
@@ -192,15 +193,19 @@ int ebsd_autotune(ebsd_handle* h, const ebsd_epilogue* e, int64_t n_sample,
                   const char* cache_path, int32_t* tile_y, int32_t* orient_per_cta,
                   float* us_per_pattern);
 
-/* Many pattern loops of uneven size in one persistent launch (no reference
+/* Many pattern loops of uneven size as one unit of work (no reference
  * counterpart: the reference runs one detector per process).  Jobs may
  * differ in detector size, binning, epilogue, orientation count and master
- * (phase); all sources must be on h's device.  A device work queue of
- * (job, 32x8-pixel tile, run of orientations) items is consumed by one
- * persistent grid (one launch per distinct energy-bin count).  With
- * EBSD_BATCH_GRAPH the table upload, queue reset and launches are captured
- * in a CUDA graph on first use and replayed for later batches with the same
- * number of jobs.  Runs on h's stream; returns when the work is queued. */
+ * (phase); all sources must be on h's device.  A job whose own launch would
+ * fill the GPU several times over (at least 64 CTAs per SM at its source
+ * handle's launch shape, e.g. the autotuner's) runs as that launch; the
+ * others share a device work queue of (job, 32 x 4 or 32 x 8-pixel tile,
+ * run of orientations) items consumed by a persistent grid (one launch per
+ * energy-bin count, noise and tile height).  With EBSD_BATCH_GRAPH all of it
+ * (table upload, queue reset, launches) is captured in a CUDA graph on first
+ * use and replayed for later batches with the same queue shape and the same
+ * large-job parameters.  Runs on h's stream; returns when the work is
+ * queued.  Records equal those of ebsd_forward on the source handles. */
 int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_t njobs, int32_t flags);
 
 /* Adjoint modes of ebsd_vjp. */

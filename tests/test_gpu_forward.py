@@ -82,6 +82,27 @@ def test_tiny_reference_weights_mode(built):
     h.close()
 
 
+@pytest.mark.parametrize("binning", [2, 4, 8])
+def test_reference_order_binning(built, binning):
+    """strict_order keeps the block sums of CTEMEBSD.f90:636 in the
+    reference's order (x fastest, one addition at a time), whether the
+    block is summed within a warp (2, 4) or through shared memory (8)."""
+    O = _oracle()
+    wl = synth.tiny(seed=9, numsx=64, numsy=48)
+    h, det, sr, num_el = _setup(wl, fp64=False)
+    h.set_option("strict_order", 1)
+    q = wl.quaternions(wl.n_orient)
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    gpu = h.forward(q, capi.epilogue(pref, binning=binning, scalingmode="lin"))
+    p32 = det.patterns_f32(sr, q, pref)
+    ref = np.stack([O.epilogue_f32(p, binning, 1, 1.0) for p in p32])
+    assert gpu.shape == ref.shape
+    l2, mx = rel_errors(gpu, ref)
+    assert mx.max() <= 1e-5, mx.max()
+    assert np.mean(gpu == ref) > 0.5
+    h.close()
+
+
 def test_c1_parity(built):
     """80x60 detector, 501^2 x 11 master, 100 orientations, gamma 0.33."""
     O = _oracle()
