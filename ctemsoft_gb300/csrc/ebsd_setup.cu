@@ -223,53 +223,68 @@ cudaError_t launch_weights(const float4* rg, int P, const int32_t* accum_e, int 
 
 // num_el = nint(sum(accum_e_detector)), CTEMEBSD.f90:516.  gfortran sums
 // the array sequentially in single precision in memory order (bin fastest,
-// then x, then y); bins outside the window add exact zeros.  That order is
-// one dependent chain of adds, so one lane performs it; the warp stages the
-// next chunk of 32 pixels through shared memory (double-buffered) so the
-// chain never waits on global memory.  Runs once per detector.
-constexpr int kNumElChunk = 32;
-
-__global__ void k_num_el(const float4* __restrict__ W, int P, int nsel, int NV,
-                         float* __restrict__ out)
+// then x, then y); bins outside the window add exact zeros, and so do the
+// zero-padded bins of the last float4 (s + 0 = s, s is never -0).  That order
+// is one dependent chain of adds, which thread 0 runs out of shared memory
+// while the whole CTA stages the next chunk of pixels (coalesced loads,
+// double-buffered), so the chain runs at the add latency.  Runs once per
+// detector.
+template <int NV>
+__global__ void __launch_bounds__(1024) k_num_el(const float4* __restrict__ W, int P,
+                                                 float* __restrict__ out)
 {
-    extern __shared__ float4 stage[];  // [2][NV][32]
-    const int lane = threadIdx.x;
-    const int nchunks = (P + kNumElChunk - 1) / kNumElChunk;
+    constexpr int CH = 3072 / NV;            // pixels per chunk: 2 x 48 KB of float4
+    extern __shared__ float4 stage[];        // [2][CH][NV]
+    const int nch = (P + CH - 1) / CH;
     auto load = [&](int ch, int buf) {
-        const int p = ch * kNumElChunk + lane;
-        for (int c = 0; c < NV; ++c)
-            stage[(buf * NV + c) * kNumElChunk + lane] =
+        for (int i = threadIdx.x; i < CH * NV; i += blockDim.x) {
+            const int c = i / CH, j = i - c * CH;  // plane by plane: coalesced
+            const int p = ch * CH + j;
+            stage[(buf * CH + j) * NV + c] =
                 p < P ? W[(int64_t)c * P + p] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
     };
     float s = 0.0f;
-    if (nchunks > 0) load(0, 0);
-    __syncwarp();
-    for (int ch = 0; ch < nchunks; ++ch) {
-        const int buf = ch & 1;
-        if (ch + 1 < nchunks) load(ch + 1, buf ^ 1);
-        if (lane == 0) {
-            const int np = min(kNumElChunk, P - ch * kNumElChunk);
-            for (int j = 0; j < np; ++j) {
-                for (int c = 0; c < NV; ++c) {
-                    const float4 w = stage[(buf * NV + c) * kNumElChunk + j];
-                    const int k = 4 * c;
-                    if (k + 0 < nsel) s = s + w.x;
-                    if (k + 1 < nsel) s = s + w.y;
-                    if (k + 2 < nsel) s = s + w.z;
-                    if (k + 3 < nsel) s = s + w.w;
-                }
+    if (nch > 0) load(0, 0);
+    __syncthreads();
+    for (int ch = 0; ch < nch; ++ch) {
+        if (ch + 1 < nch) load(ch + 1, (ch + 1) & 1);
+        if (threadIdx.x == 0) {
+            const float4* v = stage + (ch & 1) * CH * NV;
+#pragma unroll 4
+            for (int k = 0; k < CH * NV; ++k) {
+                const float4 w = v[k];
+                s = s + w.x;
+                s = s + w.y;
+                s = s + w.z;
+                s = s + w.w;
             }
         }
-        __syncwarp();
+        __syncthreads();
     }
-    if (lane == 0) *out = s;
+    if (threadIdx.x == 0) *out = s;
 }
 
 cudaError_t launch_num_el(const float4* W, int P, int nsel, int NV, float* sum_out,
                           cudaStream_t s)
 {
-    const size_t smem = sizeof(float4) * 2 * NV * kNumElChunk;
-    k_num_el<<<1, 32, smem, s>>>(W, P, nsel, NV, sum_out);
+    (void)nsel;  // bins past nsel are zero in W
+    switch (NV) {
+#define EBSD_NUM_EL(n)                                                                    \
+    case n: {                                                                             \
+        const int bytes = (int)(sizeof(float4) * 2 * (3072 / n) * n);                    \
+        const cudaError_t e = cudaFuncSetAttribute(                                       \
+            k_num_el<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);             \
+        if (e != cudaSuccess) return e;                                                   \
+        k_num_el<n><<<1, 1024, bytes, s>>>(W, P, sum_out);                                \
+        break;                                                                            \
+    }
+        EBSD_NUM_EL(1) EBSD_NUM_EL(2) EBSD_NUM_EL(3) EBSD_NUM_EL(4) EBSD_NUM_EL(5) EBSD_NUM_EL(6)
+        EBSD_NUM_EL(7) EBSD_NUM_EL(8) EBSD_NUM_EL(9) EBSD_NUM_EL(10) EBSD_NUM_EL(11)
+        EBSD_NUM_EL(12) EBSD_NUM_EL(13) EBSD_NUM_EL(14) EBSD_NUM_EL(15) EBSD_NUM_EL(16)
+#undef EBSD_NUM_EL
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

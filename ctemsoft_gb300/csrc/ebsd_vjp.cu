@@ -71,10 +71,11 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     const int iy0 = lambert_cell(prm.scl * LY, prm.npy, dy, niy);
     const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
     const float dxm = 1.0f - dx, dym = 1.0f - dy;
-    const float4* m00 = prm.master + ((int64_t)iy0 * prm.gx + ix0) * NV;
-    const float4* m10 = prm.master + ((int64_t)iy0 * prm.gx + ix1) * NV;
-    const float4* m01 = prm.master + ((int64_t)iy1 * prm.gx + ix0) * NV;
-    const float4* m11 = prm.master + ((int64_t)iy1 * prm.gx + ix1) * NV;
+    // node offsets in 32 bits: ebsd_set_master keeps the master below 2^31 float4
+    const float4* m00 = prm.master + (uint32_t)(iy0 * prm.gx + ix0) * (uint32_t)NV;
+    const float4* m10 = prm.master + (uint32_t)(iy0 * prm.gx + ix1) * (uint32_t)NV;
+    const float4* m01 = prm.master + (uint32_t)(iy1 * prm.gx + ix0) * (uint32_t)NV;
+    const float4* m11 = prm.master + (uint32_t)(iy1 * prm.gx + ix1) * (uint32_t)NV;
     // Weighted corner sums SA = sum_k W_k A_k etc. give P and both bilinear
     // slopes with four FMAs per bin; the weight derivatives need the
     // per-bin bilinear value bv.
@@ -82,14 +83,17 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     float SA = 0.0f, SB = 0.0f, SC = 0.0f, SD = 0.0f, gW0 = 0.0f, gW1 = 0.0f, gW2 = 0.0f;
     // one float4 group of bins at a time: unrolling would hoist all
     // 8*NV vector loads and spill
+    const float4* wp = prm.W + p;           // plane c of W at wp + c P
+    const float4* ep = vp.dW + p;           // plane (a NV + c) of dW
+    const int64_t plane = prm.P, eplane = (int64_t)NV * prm.P;
 #pragma unroll 1
-    for (int c = 0; c < NV; ++c) {
+    for (int c = 0; c < NV; ++c, wp += plane, ep += plane) {
         const float4 A = ldg4_keep(m00 + c, pol), B = ldg4_keep(m10 + c, pol),
                      C = ldg4_keep(m01 + c, pol), D = ldg4_keep(m11 + c, pol);
-        const float4 wc = ldg4_keep(prm.W + (int64_t)c * prm.P + p, pol);
-        const float4 e0 = ldg4_keep(vp.dW + (int64_t)(0 * NV + c) * prm.P + p, pol);
-        const float4 e1 = ldg4_keep(vp.dW + (int64_t)(1 * NV + c) * prm.P + p, pol);
-        const float4 e2 = ldg4_keep(vp.dW + (int64_t)(2 * NV + c) * prm.P + p, pol);
+        const float4 wc = ldg4_keep(wp, pol);
+        const float4 e0 = ldg4_keep(ep, pol);
+        const float4 e1 = ldg4_keep(ep + eplane, pol);
+        const float4 e2 = ldg4_keep(ep + 2 * eplane, pol);
 #define EBSD_BIN(f)                                                                        \
 {                                                                                      \
     const float bv = fmaf(A.f, w00, fmaf(B.f, w10, fmaf(C.f, w01, D.f * w11)));         \
@@ -134,9 +138,11 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
 }
 
 // Resident CTAs per SM the register allocation is held to (256 threads
-// each); a build-time tuning knob.
+// each); a build-time tuning knob.  3 (80 registers: 6 CTAs of 32 x 4
+// pixels per SM) measured 1.5 % faster at 640x480 than 4 (64 registers,
+// which spills).
 #ifndef EBSD_VJP_MIN_BLOCKS
-#define EBSD_VJP_MIN_BLOCKS 4
+#define EBSD_VJP_MIN_BLOCKS 3
 #endif
 
 template <int NV, int MODE>
@@ -145,7 +151,8 @@ __global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
 {
     constexpr int K = MODE == EBSD_VJP_NDP ? 15 : 6;
     constexpr int KP = MODE == EBSD_VJP_NDP ? 16 : 8;
-    extern __shared__ float sm[];  // [tile_y][33] pattern tile, then [tile_y][K] warp sums
+    // [tile_y][33] pattern tile, then [opc][tile_y][K] warp sums
+    extern __shared__ float sm[];
     float* tile = sm;
     float* red = sm + 33 * tile_y;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
@@ -216,16 +223,18 @@ __global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
         }
         warp_reduce_scatter<KP>(acc, tx);
         {
+            // each warp its own slot per orientation: no barrier until the end
             const int idx = tx / (32 / KP);
-            if (tx % (32 / KP) == 0 && idx < K) red[ty * K + idx] = acc[0];
+            if (tx % (32 / KP) == 0 && idx < K) red[((o - o_begin) * tile_y + ty) * K + idx] = acc[0];
         }
-        __syncthreads();
-        if (tid < K) {
-            float s2 = 0.0f;
-            for (int wy = 0; wy < tile_y; ++wy) s2 += red[wy * K + tid];
-            vp.partial[(o * ntiles + t) * K + tid] = s2;
-        }
-        __syncthreads();
+    }
+    __syncthreads();
+    const int no = (int)min((int64_t)opc, prm.n - o_begin);
+    for (int i = tid; i < no * K; i += blockDim.x) {
+        const int ol = i / K, k = i - ol * K;
+        float s2 = 0.0f;
+        for (int wy = 0; wy < tile_y; ++wy) s2 += red[(ol * tile_y + wy) * K + k];
+        vp.partial[((o_begin + ol) * ntiles + t) * K + k] = s2;
     }
 }
 
@@ -366,15 +375,17 @@ __global__ void __launch_bounds__(256, 2) k_gn(const FwdParams prm, const VjpPar
         }
         warp_reduce_scatter<16>(acc, tx);
         warp_reduce_scatter<32>(accm, tx);
-        if (tx % 2 == 0 && tx / 2 < 15) red[ty * kGnK + tx / 2] = acc[0];
-        if (tx < 21) red[ty * kGnK + 15 + tx] = accm[0];
-        __syncthreads();
-        if (tid < kGnK) {
-            float s2 = 0.0f;
-            for (int wy = 0; wy < tile_y; ++wy) s2 += red[wy * kGnK + tid];
-            vp.partial[(o * ntiles + t) * kGnK + tid] = s2;
-        }
-        __syncthreads();
+        float* rw = red + ((o - o_begin) * tile_y + ty) * kGnK;  // this warp's slot
+        if (tx % 2 == 0 && tx / 2 < 15) rw[tx / 2] = acc[0];
+        if (tx < 21) rw[15 + tx] = accm[0];
+    }
+    __syncthreads();
+    const int no = (int)min((int64_t)opc, prm.n - o_begin);
+    for (int i = tid; i < no * kGnK; i += blockDim.x) {
+        const int ol = i / kGnK, k = i - ol * kGnK;
+        float s2 = 0.0f;
+        for (int wy = 0; wy < tile_y; ++wy) s2 += red[(ol * tile_y + wy) * kGnK + k];
+        vp.partial[((o_begin + ol) * ntiles + t) * kGnK + k] = s2;
     }
 }
 
@@ -547,7 +558,12 @@ cudaError_t launch_gn_nv(const FwdParams& p, const VjpParams& vp, int tile_y, cu
     const int opc = vp.opc;
     const int64_t blocks = ((p.n + opc - 1) / opc) * ntiles;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    const size_t smem = sizeof(float) * (33 * tile_y * 7 + kGnK * tile_y);
+    const size_t smem = sizeof(float) * (33 * tile_y * 7 + (size_t)kGnK * tile_y * opc);
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(
+            k_gn<NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     k_gn<NV><<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, vp, tile_y, tiles_x, ntiles, opc);
     return cudaGetLastError();
 }
@@ -563,7 +579,15 @@ cudaError_t launch_vjp_nv(const FwdParams& p, const VjpParams& vp, int mode, int
     const int64_t blocks = ((p.n + opc - 1) / opc) * ntiles;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     const int K = mode == EBSD_VJP_NDP ? 15 : 6;
-    const size_t smem = sizeof(float) * (33 * tile_y + K * tile_y);
+    const size_t smem = sizeof(float) * (33 * tile_y + (size_t)K * tile_y * opc);
+    if (smem > 48 * 1024) {
+        const cudaError_t e = mode == EBSD_VJP_NDP
+            ? cudaFuncSetAttribute(k_vjp<NV, EBSD_VJP_NDP>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+            : cudaFuncSetAttribute(k_vjp<NV, EBSD_VJP_COTANGENT>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     if (mode == EBSD_VJP_NDP)
         k_vjp<NV, EBSD_VJP_NDP><<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, vp, tile_y,
                                                                                tiles_x, ntiles, opc);
