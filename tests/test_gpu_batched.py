@@ -137,3 +137,45 @@ def test_autotune_and_cache(built, tmp_path):
     h3.share_master(h)
     h3.set_detector(wl.geometry(), wl.mc(), 1, 5)
     assert np.array_equal(h2.forward(q, epi), h3.forward(q, epi))
+
+
+def test_batched_large_jobs_run_as_own_launches(built):
+    """Jobs that fill the GPU by themselves run at their handle's launch
+    shape inside the batch's graph, beside the queued small jobs; records
+    equal per-job launches, also when the graph is replayed with new
+    orientations and rebuilt for a new output buffer."""
+    torch = pytest.importorskip("torch")
+    masters, jobs = _mixed_jobs(torch, seed=7)
+    mh, acc = masters["Ni"]
+    for nx, ny, n, b in ((640, 480, 400, 1), (320, 240, 3000, 2)):
+        h = capi.Handle(0)
+        h.share_master(mh)
+        geom = dict(L=15000.0, thetac=10.0, delta=12800.0 / nx, numsx=nx, numsy=ny, xpc=0.5,
+                    ypc=-0.5, sig=70.0)
+        num_el = h.set_detector(geom, acc, 1, 5)
+        epi = capi.epilogue(capi.prefactor(15.0, 100.0, num_el), binning=b, scalingmode="gam",
+                            gammavalue=0.33)
+        ox, oy = h.output_dims(epi)
+        q = torch.from_numpy(synth.shoemake_quaternions(n, 900 + n)).cuda()
+        jobs.insert(3, (h, q, epi, torch.full((n, oy, ox), -1.0, device="cuda")))
+    runner = capi.Handle(0)
+
+    def check(tag):
+        torch.cuda.synchronize()
+        for i, (h, q, epi, out) in enumerate(jobs):
+            ref = torch.empty_like(out)
+            h.forward(q, epi, out=ref)
+            torch.cuda.synchronize()
+            assert torch.equal(out, ref), f"{tag} job {i}"
+
+    runner.forward_batched(jobs, graph=True)
+    check("first")
+    for h, q, epi, out in jobs:
+        q.copy_(torch.from_numpy(synth.shoemake_quaternions(q.shape[0], 77 + q.shape[0])))
+        out.fill_(-1.0)
+    runner.forward_batched(jobs, graph=True)
+    check("replay")
+    h, q, epi, out = jobs[3]
+    jobs[3] = (h, q, epi, torch.full_like(out, -1.0))
+    runner.forward_batched(jobs, graph=True)
+    check("new buffer")
