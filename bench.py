@@ -53,9 +53,9 @@ def _args():
     ap.add_argument("--noise-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5", "mc", "dict"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "mc", "dict"],
                     help="c2: 640x480 plain forward (default); c3: 64-job batch; "
-                         "c5: Gauss-Newton refinement")
+                         "c4: 480x480 forward + adjoint; c5: Gauss-Newton refinement")
     ap.add_argument("--c3-jobs", type=int, default=64,
                     help="c3: use the first N of the 64 jobs (small profiling cases)")
     ap.add_argument("--c3-max-orient", type=int, default=0,
@@ -471,6 +471,69 @@ def _e2e(h, q, epi, N, nx, ny, args, world, dev, barrier):
                              "cudaMemcpy device-to-host into the same pinned memory"}}
 
 
+def run_c4(args):
+    """The adjoint workload: 480x480 detector, 1001^2 x 11-bin master, 4096
+    orientations; the fused forward + adjoint (loss and its gradient with
+    respect to 3 rotation tangents and the pattern centre) against the plain
+    forward of the same patterns."""
+    import torch
+
+    from ctemsoft_gb300 import capi, synth
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    wl = synth.C4
+    sr, acc = wl.master(), wl.mc()
+    q = wl.quaternions()
+    N = len(q)
+    h = capi.Handle(0)
+    h.set_master(sr)
+    num_el = h.set_detector(wl.geometry(), acc, 1, wl.nEbins)
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    epi = capi.epilogue(pref)
+    nx, ny = h.output_dims(epi)
+    tuned = h.autotune(epi, 256, Path(tempfile.gettempdir()) / "ebsd_autotune_0.txt")
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    h.set_stream(stream.cuda_stream)
+    dq = torch.from_numpy(q).to(dev)
+    dout = torch.empty((N, ny, nx), dtype=torch.float32, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        h.forward(dq, epi, out=dout)
+    torch.cuda.synchronize()
+    clocks = Clocks(0)
+    clocks.start()
+    tot = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        h.forward(dq, epi, out=dout)
+        b.record(stream)
+        torch.cuda.synchronize()
+        tot += a.elapsed_time(b)
+    fwd = N * args.steps / (tot / 1000.0)
+    vjp = _fwd_vjp(h, q, wl, pref, dout, stream, args, 1, dev, torch.cuda.synchronize, fwd)
+    ck = clocks.stop()
+    line = {
+        "metric": "EBSD fused forward + adjoint patterns/s (480x480, 4096 orientations)",
+        "value": vjp["value"], "unit": UNIT, "n_gpus": 1, "steps": args.vjp_steps,
+        "warmup": args.warmup, "ms_per_step": vjp["ms_per_step"], "higher_is_better": True,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.name, "detector": f"{wl.numsx}x{wl.numsy}",
+                   "master": f"{2 * wl.npx + 1}^2 x {wl.nEbins} bins", "orientations": N,
+                   "l2": "flushed between the forward's timed steps"},
+        "forward": {"value": fwd, "unit": UNIT, "steps": args.steps,
+                    "launch_shape": {"tile_y": tuned[0], "orient_per_cta": tuned[1]}},
+        "ratio_to_forward": vjp["ratio_to_forward"], "what": vjp["what"],
+        "mean_loss": vjp["mean_loss"], "finite": vjp["finite"],
+        "gpu_launches": 2 * args.vjp_steps, "clocks": ck,
+    }
+    print(json.dumps(line))
+    h.close()
+    return 0
+
+
 def run_batched(args):
     """The batched uneven workload: 64 jobs (seed 2) of mixed detector size,
     binning, orientation count and phase in one persistent launch replayed
@@ -884,6 +947,8 @@ def main():
         return run_reference(args)
     if args.workload == "c3":
         return run_batched(args)
+    if args.workload == "c4":
+        return run_c4(args)
     if args.workload == "c5":
         return run_gn(args)
     if args.workload == "mc":
