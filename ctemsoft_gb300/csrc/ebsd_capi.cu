@@ -62,7 +62,7 @@ struct ebsd_handle {
     float4* d_rg = nullptr;
     float4* d_W = nullptr;
     float4* d_drg = nullptr;   // [3][P] d rg / d(xpc, ypc, L)
-    float4* d_dW = nullptr;    // [3][NV][P] d W / d(xpc, ypc, L)
+    float4* d_dW = nullptr;    // [2NV+1][P] factors of d W / d(xpc, ypc, L) (see VjpParams)
     int P = 0;
     int nsx = 0, nsy = 0;
 
@@ -535,7 +535,7 @@ int detector_setup(ebsd_handle* h, const ebsd_geometry* g, bool with_num_el)
         CK(h, cudaMalloc(&h->d_rg, sizeof(float4) * (size_t)P), "cudaMalloc rg");
         CK(h, cudaMalloc(&h->d_W, sizeof(float4) * (size_t)P * NV), "cudaMalloc W");
         CK(h, cudaMalloc(&h->d_drg, sizeof(float4) * (size_t)P * 3), "cudaMalloc drg");
-        CK(h, cudaMalloc(&h->d_dW, sizeof(float4) * (size_t)P * 3 * NV), "cudaMalloc dW");
+        CK(h, cudaMalloc(&h->d_dW, sizeof(float4) * (size_t)P * (2 * NV + 1)), "cudaMalloc dW");
     }
     const int32_t* acc = (const int32_t*)h->accum.ptr;
     float ca, sa;

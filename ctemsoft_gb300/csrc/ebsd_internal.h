@@ -52,7 +52,8 @@ struct FwdParams {
 // the current chunk of orientations by the caller.
 struct VjpParams {
     const float4* drg;   // [3][P] d rg / d(xpc, ypc, L)
-    const float4* dW;    // [3][NV][P] d W / d(xpc, ypc, L)
+    const float4* dW;    // [2NV+1][P]: dW/d(xpc, ypc, L) = G0 di0 + G1 di1; planes
+                         // 0..NV-1 G0, NV..2NV-1 G1, 2NV di1 (di0 in drg's .w)
     const float* data;   // [n][out_ny][out_nx] cotangent or targets
     float* partial;      // scratch [n][ntiles][K]
     float* loss;         // [n] or null

@@ -320,7 +320,7 @@ __global__ void k_geom_derivs(WeightsGeom gd, const int32_t* __restrict__ acc, i
         const double pr = r[0] * dv[a][0] + r[1] * dv[a][1] + r[2] * dv[a][2];
         for (int c = 0; c < 3; ++c) dr[a][c] = (dv[a][c] - pr * r[c]) / nv;
         drg[(int64_t)a * P + p] = make_float4((float)dr[a][0], (float)dr[a][1], (float)dr[a][2],
-                                              0.0f);
+                                              0.0f);  // .w: d Dx / d theta_a, below
     }
     // MC Lambert point and its Jacobian (Lambert.f90:452-483 differentiated)
     double x = r[0], y = r[1], z = r[2], sm = 1.0;
@@ -370,24 +370,27 @@ __global__ void k_geom_derivs(WeightsGeom gd, const int32_t* __restrict__ acc, i
     const int32_t* a10 = acc + ((int64_t)jy0 * gxm + jx1) * nE + e0;
     const int32_t* a01 = acc + ((int64_t)jy1 * gxm + jx0) * nE + e0;
     const int32_t* a11 = acc + ((int64_t)jy1 * gxm + jx1) * nE + e0;
-    for (int a = 0; a < 3; ++a) {
-        for (int c = 0; c < NV; ++c) {
-            float u[4];
-            for (int t = 0; t < 4; ++t) {
-                const int k = 4 * c + t;
-                double g = 0.0;
-                if (k < nsel) {
-                    const double g0 = 0.25 * ((double)(a10[k] - a00[k]) * Dym +
-                                              (double)(a11[k] - a01[k]) * Dy);
-                    const double g1 = 0.25 * ((double)(a01[k] - a00[k]) * Dxm +
-                                              (double)(a11[k] - a10[k]) * Dx);
-                    g = g0 * di0[a] + g1 * di1[a];
-                }
-                u[t] = (float)g;
+    // dW_k / d theta_a = G0_k di0[a] + G1_k di1[a]: the slopes of the bilinear
+    // weight along the two MC grid axes (planes 0..NV-1 and NV..2NV-1 of dW)
+    // and the derivatives of the grid fractions (di0 in the drg planes' w,
+    // di1 in plane 2NV of dW)
+    for (int c = 0; c < NV; ++c) {
+        float u0[4], u1[4];
+        for (int t = 0; t < 4; ++t) {
+            const int k = 4 * c + t;
+            double g0 = 0.0, g1 = 0.0;
+            if (k < nsel) {
+                g0 = 0.25 * ((double)(a10[k] - a00[k]) * Dym + (double)(a11[k] - a01[k]) * Dy);
+                g1 = 0.25 * ((double)(a01[k] - a00[k]) * Dxm + (double)(a11[k] - a10[k]) * Dx);
             }
-            dW[((int64_t)a * NV + c) * P + p] = make_float4(u[0], u[1], u[2], u[3]);
+            u0[t] = (float)g0;
+            u1[t] = (float)g1;
         }
+        dW[(int64_t)c * P + p] = make_float4(u0[0], u0[1], u0[2], u0[3]);
+        dW[(int64_t)(NV + c) * P + p] = make_float4(u1[0], u1[1], u1[2], u1[3]);
     }
+    for (int a = 0; a < 3; ++a) drg[(int64_t)a * P + p].w = (float)di0[a];
+    dW[(int64_t)(2 * NV) * P + p] = make_float4((float)di1[0], (float)di1[1], (float)di1[2], 0.0f);
 }
 
 cudaError_t launch_geom_derivs(const ebsd_geometry& g, const int32_t* accum_e, int nE, int nsx,

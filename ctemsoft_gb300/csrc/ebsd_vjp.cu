@@ -47,6 +47,35 @@ __device__ __forceinline__ void warp_reduce_scatter(float (&v)[KP], int lane)
     for (; off > 0; off >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
 }
 
+// Pixel (tx, ty) of thread tid in a 32-wide tile.  BSH (binning 2 or 4):
+// each warp covers a 32/b x b block, so every binning block lies within one
+// warp and is summed with shuffles (adj_block_sum); otherwise warps are rows.
+// The kernels take BSH as a template argument, so that the unbinned variant
+// carries none of it (a runtime test cost 3 % at 640x480).
+template <bool BSH>
+__device__ __forceinline__ void adj_pixel(int tid, int b, int& tx, int& ty)
+{
+    const int lane = tid & 31, wid = tid >> 5;
+    if (BSH) {
+        const int bw = 32 / b;  // warps per tile row: kTileX / bw = b
+        tx = (wid % b) * bw + lane % bw;
+        ty = (wid / b) * b + lane / bw;
+    } else {
+        tx = lane;
+        ty = wid;
+    }
+}
+
+// Sum of v over the b x b binning block that holds this lane (b = 2 or 4,
+// warp = 32/b x b lanes, row-major); every lane of the block gets the total.
+__device__ __forceinline__ float adj_block_sum(float v, int b)
+{
+    const int bw = 32 / b;
+    for (int m = 1; m < b; m <<= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+    for (int m = 1; m < b; m <<= 1) v += __shfl_xor_sync(0xffffffffu, v, m * bw);
+    return v;
+}
+
 // Value and the six derivatives (w0, w1, w2, xpc, ypc, L) of output pixel p
 // of orientation o, before binning.
 template <int NV>
@@ -80,11 +109,13 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     // slopes with four FMAs per bin; the weight derivatives need the
     // per-bin bilinear value bv.
     const float w00 = dxm * dym, w10 = dx * dym, w01 = dxm * dy, w11 = dx * dy;
-    float SA = 0.0f, SB = 0.0f, SC = 0.0f, SD = 0.0f, gW0 = 0.0f, gW1 = 0.0f, gW2 = 0.0f;
+    float SA = 0.0f, SB = 0.0f, SC = 0.0f, SD = 0.0f, U0 = 0.0f, U1 = 0.0f;
     // one float4 group of bins at a time: unrolling would hoist all
     // 8*NV vector loads and spill
+    // dW_k/dtheta_a = G0_k di0_a + G1_k di1_a, so the weight terms need only
+    // U0 = sum_k G0_k bv_k and U1 = sum_k G1_k bv_k
     const float4* wp = prm.W + p;           // plane c of W at wp + c P
-    const float4* ep = vp.dW + p;           // plane (a NV + c) of dW
+    const float4* ep = vp.dW + p;           // plane c of G0; G1 NV planes further
     const int64_t plane = prm.P, eplane = (int64_t)NV * prm.P;
 #pragma unroll 1
     for (int c = 0; c < NV; ++c, wp += plane, ep += plane) {
@@ -93,7 +124,6 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
         const float4 wc = ldg4_keep(wp, pol);
         const float4 e0 = ldg4_keep(ep, pol);
         const float4 e1 = ldg4_keep(ep + eplane, pol);
-        const float4 e2 = ldg4_keep(ep + 2 * eplane, pol);
 #define EBSD_BIN(f)                                                                        \
 {                                                                                      \
     const float bv = fmaf(A.f, w00, fmaf(B.f, w10, fmaf(C.f, w01, D.f * w11)));         \
@@ -101,9 +131,8 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     SB = fmaf(wc.f, B.f, SB);                                                           \
     SC = fmaf(wc.f, C.f, SC);                                                           \
     SD = fmaf(wc.f, D.f, SD);                                                           \
-    gW0 = fmaf(e0.f, bv, gW0);                                                          \
-    gW1 = fmaf(e1.f, bv, gW1);                                                          \
-    gW2 = fmaf(e2.f, bv, gW2);                                                          \
+    U0 = fmaf(e0.f, bv, U0);                                                            \
+    U1 = fmaf(e1.f, bv, U1);                                                            \
 }
         EBSD_BIN(x) EBSD_BIN(y) EBSD_BIN(z) EBSD_BIN(w)
 #undef EBSD_BIN
@@ -132,9 +161,10 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     const float m2 = q.x * u3 - q.y * u2 + q.z * u1 - q.w * u0;
     const float4 r0 = ldg4_keep(vp.drg + p, pol), r1 = ldg4_keep(vp.drg + prm.P + p, pol),
                  r2 = ldg4_keep(vp.drg + 2 * (int64_t)prm.P + p, pol);
-    J[3] = m0 * r0.x + m1 * r0.y + m2 * r0.z + pref * gW0;
-    J[4] = m0 * r1.x + m1 * r1.y + m2 * r1.z + pref * gW1;
-    J[5] = m0 * r2.x + m1 * r2.y + m2 * r2.z + pref * gW2;
+    const float4 di1 = ldg4_keep(vp.dW + 2 * eplane + p, pol);  // (xpc, ypc, L)
+    J[3] = m0 * r0.x + m1 * r0.y + m2 * r0.z + pref * fmaf(U0, r0.w, U1 * di1.x);
+    J[4] = m0 * r1.x + m1 * r1.y + m2 * r1.z + pref * fmaf(U0, r1.w, U1 * di1.y);
+    J[5] = m0 * r2.x + m1 * r2.y + m2 * r2.z + pref * fmaf(U0, r2.w, U1 * di1.z);
 }
 
 // Resident CTAs per SM the register allocation is held to (256 threads
@@ -145,7 +175,7 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
 #define EBSD_VJP_MIN_BLOCKS 3
 #endif
 
-template <int NV, int MODE>
+template <int NV, int MODE, bool BSH>
 __global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
     k_vjp(const FwdParams prm, const VjpParams vp, int tile_y, int tiles_x, int ntiles, int opc)
 {
@@ -155,7 +185,9 @@ __global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
     extern __shared__ float sm[];
     float* tile = sm;
     float* red = sm + 33 * tile_y;
-    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    int tx, ty;
+    adj_pixel<BSH>(tid, vp.binning, tx, ty);
     // Orientation blocks vary fastest across the grid: the CTAs resident at
     // any moment cover a few tiles for many orientations, so each tile's
     // per-pixel tables (W, dW, rg, drg: larger than L2 together with the
@@ -185,7 +217,9 @@ __global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
         if (inside) pixel_value_jacobian<NV>(prm, vp, p, o, pol, pref, val, J);
         // output-record value of this pixel's block
         float O = val;
-        if (b > 1) {
+        if (BSH) {
+            O = adj_block_sum(val, b) * ib2;
+        } else if (b > 1) {
             tile[ty * 33 + tx] = val;
             __syncthreads();
             if (inside) {
@@ -221,11 +255,11 @@ __global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
 #pragma unroll
             for (int a = 0; a < K; ++a) acc[a] = 0.0f;
         }
-        warp_reduce_scatter<KP>(acc, tx);
+        warp_reduce_scatter<KP>(acc, lane);
         {
             // each warp its own slot per orientation: no barrier until the end
-            const int idx = tx / (32 / KP);
-            if (tx % (32 / KP) == 0 && idx < K) red[((o - o_begin) * tile_y + ty) * K + idx] = acc[0];
+            const int idx = lane / (32 / KP);
+            if (lane % (32 / KP) == 0 && idx < K) red[((o - o_begin) * tile_y + wid) * K + idx] = acc[0];
         }
     }
     __syncthreads();
@@ -291,7 +325,7 @@ __device__ __forceinline__ int pk(int i, int j)  // packed index of H(i,j), i <=
     return i * 6 - (i * (i - 1)) / 2 + (j - i);
 }
 
-template <int NV>
+template <int NV, bool BSH>
 __global__ void __launch_bounds__(256, 2) k_gn(const FwdParams prm, const VjpParams vp,
                                                int tile_y, int tiles_x, int ntiles, int opc)
 {
@@ -299,7 +333,9 @@ __global__ void __launch_bounds__(256, 2) k_gn(const FwdParams prm, const VjpPar
     float* tile = sm;
     float* jt = sm + 33 * tile_y;
     float* red = jt + 6 * 33 * tile_y;
-    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    int tx, ty;
+    adj_pixel<BSH>(tid, vp.binning, tx, ty);
     // Orientation blocks vary fastest across the grid: the CTAs resident at
     // any moment cover a few tiles for many orientations, so each tile's
     // per-pixel tables (W, dW, rg, drg: larger than L2 together with the
@@ -326,7 +362,11 @@ __global__ void __launch_bounds__(256, 2) k_gn(const FwdParams prm, const VjpPar
         float O = val, JB[6];
 #pragma unroll
         for (int a = 0; a < 6; ++a) JB[a] = J[a];
-        if (b > 1) {
+        if (BSH) {  // block sums within the warp
+            O = adj_block_sum(val, b) * ib2;
+#pragma unroll
+            for (int a = 0; a < 6; ++a) JB[a] = adj_block_sum(J[a], b) * ib2;
+        } else if (b > 1) {
             tile[ty * 33 + tx] = val;
 #pragma unroll
             for (int a = 0; a < 6; ++a) jt[(a * tile_y + ty) * 33 + tx] = inside ? J[a] : 0.0f;
@@ -373,11 +413,11 @@ __global__ void __launch_bounds__(256, 2) k_gn(const FwdParams prm, const VjpPar
                     for (int j = i; j < 6; ++j) accm[pk(i, j)] = JB[i] * JB[j];
             }
         }
-        warp_reduce_scatter<16>(acc, tx);
-        warp_reduce_scatter<32>(accm, tx);
-        float* rw = red + ((o - o_begin) * tile_y + ty) * kGnK;  // this warp's slot
-        if (tx % 2 == 0 && tx / 2 < 15) rw[tx / 2] = acc[0];
-        if (tx < 21) rw[15 + tx] = accm[0];
+        warp_reduce_scatter<16>(acc, lane);
+        warp_reduce_scatter<32>(accm, lane);
+        float* rw = red + ((o - o_begin) * tile_y + wid) * kGnK;  // this warp's slot
+        if (lane % 2 == 0 && lane / 2 < 15) rw[lane / 2] = acc[0];
+        if (lane < 21) rw[15 + lane] = accm[0];
     }
     __syncthreads();
     const int no = (int)min((int64_t)opc, prm.n - o_begin);
@@ -549,6 +589,14 @@ __global__ void k_gn_update(const double* __restrict__ sys, int64_t n, double la
     quats[o] = make_float4((float)(r0 / nq), (float)(r1 / nq), (float)(r2 / nq), (float)(r3 / nq));
 }
 
+// Dynamic shared memory above the default 48 KB needs the kernel's opt-in.
+template <typename Kern>
+cudaError_t allow_smem(Kern kern, size_t bytes)
+{
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
 template <int NV>
 cudaError_t launch_gn_nv(const FwdParams& p, const VjpParams& vp, int tile_y, cudaStream_t s)
 {
@@ -559,13 +607,14 @@ cudaError_t launch_gn_nv(const FwdParams& p, const VjpParams& vp, int tile_y, cu
     const int64_t blocks = ((p.n + opc - 1) / opc) * ntiles;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     const size_t smem = sizeof(float) * (33 * tile_y * 7 + (size_t)kGnK * tile_y * opc);
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(
-            k_gn<NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const bool bsh = vp.binning == 2 || vp.binning == 4;
+    auto go = [&](auto kern) {
+        const cudaError_t e = allow_smem(kern, smem);
         if (e != cudaSuccess) return e;
-    }
-    k_gn<NV><<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, vp, tile_y, tiles_x, ntiles, opc);
-    return cudaGetLastError();
+        kern<<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, vp, tile_y, tiles_x, ntiles, opc);
+        return cudaGetLastError();
+    };
+    return bsh ? go(k_gn<NV, true>) : go(k_gn<NV, false>);
 }
 
 template <int NV>
@@ -580,21 +629,17 @@ cudaError_t launch_vjp_nv(const FwdParams& p, const VjpParams& vp, int mode, int
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     const int K = mode == EBSD_VJP_NDP ? 15 : 6;
     const size_t smem = sizeof(float) * (33 * tile_y + (size_t)K * tile_y * opc);
-    if (smem > 48 * 1024) {
-        const cudaError_t e = mode == EBSD_VJP_NDP
-            ? cudaFuncSetAttribute(k_vjp<NV, EBSD_VJP_NDP>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-            : cudaFuncSetAttribute(k_vjp<NV, EBSD_VJP_COTANGENT>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const bool bsh = vp.binning == 2 || vp.binning == 4;
+    auto go = [&](auto kern) {
+        const cudaError_t e = allow_smem(kern, smem);
         if (e != cudaSuccess) return e;
-    }
+        kern<<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, vp, tile_y, tiles_x, ntiles, opc);
+        return cudaGetLastError();
+    };
     if (mode == EBSD_VJP_NDP)
-        k_vjp<NV, EBSD_VJP_NDP><<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(p, vp, tile_y,
-                                                                               tiles_x, ntiles, opc);
-    else
-        k_vjp<NV, EBSD_VJP_COTANGENT><<<(unsigned)blocks, kTileX * tile_y, smem, s>>>(
-            p, vp, tile_y, tiles_x, ntiles, opc);
-    return cudaGetLastError();
+        return bsh ? go(k_vjp<NV, EBSD_VJP_NDP, true>) : go(k_vjp<NV, EBSD_VJP_NDP, false>);
+    return bsh ? go(k_vjp<NV, EBSD_VJP_COTANGENT, true>)
+               : go(k_vjp<NV, EBSD_VJP_COTANGENT, false>);
 }
 
 }  // namespace
