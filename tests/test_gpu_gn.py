@@ -48,7 +48,7 @@ def _problem(torch, binning=1, n=64, pc_shift=(0.0, 0.0, 0.0)):
     return wl, h, epi, qt, targets, true_geom
 
 
-@pytest.mark.parametrize("binning", [1, 4])
+@pytest.mark.parametrize("binning", [1, 2, 4, 8])
 def test_refine_orientations(built, binning):
     torch = pytest.importorskip("torch")
     wl, h, epi, qt, targets, _ = _problem(torch, binning)

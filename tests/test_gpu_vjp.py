@@ -51,7 +51,7 @@ def _targets(O, wl, sr, acc, q, b):
     return T.astype(np.float32)
 
 
-@pytest.mark.parametrize("binning", [1, 2, 4])
+@pytest.mark.parametrize("binning", [1, 2, 4, 8])
 def test_ndp_matches_fp64_analytic(built, binning):
     from oracle import oracle as O
     wl = _wl()
