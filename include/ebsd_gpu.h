@@ -126,7 +126,7 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *   "mc_fp32"        0 (default): ebsd_mc_run in binary64, the reference's
  *                    arithmetic; 1: the same trajectory steps in binary32,
  *                    statistically equivalent and, since GB300's binary64
- *                    units bound the default, about 16x faster (62.9 M vs
+ *                    units bound the default, about 16x faster (62.6 M vs
  *                    3.8 M electrons/s at the CTEMMC defaults). */
 int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value);
 
