@@ -7,10 +7,10 @@
 // Dror and Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC 2011)
 // keyed by the seed, with the counter (pattern index, pixel index), so the
 // noise does not depend on launch shape, chunking or device.  The sampler
-// is inversion by sequential search for small means and Hormann's
-// transformed rejection with squeeze, PTRS ("The transformed rejection
-// method for generating Poisson random variables", Insurance: Mathematics
-// and Economics 12, 1993), for means >= 10.
+// is inversion by sequential search for means below kInversionMax and
+// Hormann's transformed rejection with squeeze, PTRS ("The transformed
+// rejection method for generating Poisson random variables", Insurance:
+// Mathematics and Economics 12, 1993; valid for means >= 10) above.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -116,18 +116,31 @@ __device__ __forceinline__ float log_poisson_pmf(float k, float lambda, float lo
            ik * ik * ik * (1.0f / 360.0f);
 }
 
+// Inversion below this mean, PTRS from it on (PTRS needs means >= 10).  A
+// warp runs every branch that one of its lanes takes, so where a pattern's
+// means straddle the split both branches run; measured on 640x480 patterns
+// over five intensity scales (means ~1 to ~100), a split at 10 is the best
+// compromise: 20 or 30 gain 2-9 % at means near 10 and lose 13-25 % at
+// means of 30-100, where the long sequential searches of the dim pixels
+// hold up warps of PTRS draws.
+constexpr float kInversionMax = 10.0f;
+
 // One Poisson(lambda) draw.  lambda <= 0 (or NaN) gives 0.
 __device__ __forceinline__ float poisson_draw(float lambda, PixelRng& rng)
 {
     if (!(lambda > 0.0f)) return 0.0f;
-    if (lambda < 10.0f) {
-        // inversion: walk the cumulative distribution from k = 0
+    if (lambda < kInversionMax) {
+        // inversion: walk the cumulative distribution from k = 0.  Rounding
+        // can leave the single-precision sum a little below 1; a u above it
+        // ends the walk where the terms no longer move the sum (deep in the
+        // tail, probability ~1e-7) instead of running on to the cap.
         const float u = rng.next();
         float p = __expf(-lambda), cdf = p;
         int k = 0;
         while (u > cdf && k < 200) {
             ++k;
             p *= __fdividef(lambda, (float)k);
+            if (p <= 5.9604645e-8f * cdf) break;  // 2^-24 of the sum
             cdf += p;
         }
         return (float)k;

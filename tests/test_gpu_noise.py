@@ -72,7 +72,7 @@ def test_poisson_reproducible_and_chunk_independent(built):
     np.testing.assert_allclose(g, ref, rtol=2e-6)
 
 
-@pytest.mark.parametrize("lam", [12.5, 340.0, 2.0e4, 1.0e6])
+@pytest.mark.parametrize("lam", [12.5, 27.0, 29.5, 34.0, 340.0, 2.0e4, 1.0e6])
 def test_poisson_distribution_shape(built, lam):
     """The whole distribution, not only its moments: a uniform master with
     uniform weights gives every pixel nearly the same mean, and 614 k draws are
