@@ -87,6 +87,16 @@ def _traffic_per_pattern():
     return float(m.group(1)) if m else None
 
 
+def _l1_wavefront_frac():
+    """The pattern kernel's L1 data-pipe wavefront rate (fraction of peak)
+    from the committed ncu summary, or None."""
+    f = ROOT / "profiles" / "k_forward_640x480.md"
+    if not f.exists():
+        return None
+    m = re.search(r"L1 data-pipe wavefronts \(LSU\) \| ([0-9.]+) %", f.read_text())
+    return float(m.group(1)) / 100.0 if m else None
+
+
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons."""
 
@@ -362,7 +372,10 @@ def run_ours(args):
                          "traffic": (tpp * N if tpp else None),
                          "algorithmic_bytes_per_pattern": b_pattern,
                          "note": "gathered master bytes are served by L1/L2 (master is "
-                                 "L2-resident), so frac can exceed 1"},
+                                 "L2-resident), so frac can exceed 1",
+                         "binding_unit": {"unit": "L1 data pipe (LSU wavefronts)",
+                                          "frac": _l1_wavefront_frac(),
+                                          "source": "profiles/k_forward_640x480.md"}},
             "e2e": e2e,
             "fwd_vjp": fwd_vjp,
             "fwd_noise": fwd_noise,

@@ -72,6 +72,7 @@ struct ebsd_handle {
     DeviceBuf tmp;
     DeviceBuf accum;           // MC histogram, kept for geometry updates
     DeviceBuf small;           // set-up scalars (num_el sum)
+    DeviceBuf wref;            // the reference's single-precision weights (num_el)
     DeviceBuf vjp_partial;     // per-CTA partial sums of the adjoint
     DeviceBuf gn_sys;          // per-pattern Gauss-Newton systems (28 doubles)
     DeviceBuf gn_aux;          // Schur partials, centre system, centre step, steps
@@ -352,6 +353,7 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
     cudaFree(h->tmp.ptr);
     cudaFree(h->accum.ptr);
     cudaFree(h->small.ptr);
+    cudaFree(h->wref.ptr);
     cudaFree(h->gn_sys.ptr);
     cudaFree(h->gn_aux.ptr);
     cudaFree(h->batch_table.ptr);
@@ -542,8 +544,11 @@ int detector_setup(ebsd_handle* h, const ebsd_geometry* g, bool with_num_el)
     host::detector_angles(g->sig, g->thetac, &ca, &sa);
     CK(h, launch_detector(*g, ca, sa, h->d_rg, s), "detector kernel");
     const float sclmc = host::lambert_scale(h->nsx);
-    float4* d_wref = nullptr;
-    CK(h, cudaMalloc(&d_wref, sizeof(float4) * (size_t)P * NV), "cudaMalloc weights");
+    // kept by the handle: a refinement of the pattern centre sets the detector
+    // up every iteration
+    int rcw = ensure(h, h->wref, sizeof(float4) * (size_t)P * NV, "reference weights");
+    if (rcw) return rcw;
+    float4* d_wref = (float4*)h->wref.ptr;
     cudaError_t e = launch_weights(h->d_rg, P, acc, h->nE, h->nsx, h->nsy, sclmc,
                                    host::lambert_spi2_f(), h->Emin - 1, nsel, NV,
                                    h->weights_fp64, *g, h->d_W, d_wref, s);
@@ -558,7 +563,6 @@ int detector_setup(ebsd_handle* h, const ebsd_geometry* g, bool with_num_el)
             e = cudaMemcpyAsync(&sum, d_sum, sizeof(float), cudaMemcpyDeviceToHost, s);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFree(d_wref);
     if (e != cudaSuccess) return cuda_err(h, e, "detector weights");
     if (with_num_el) h->num_el = (int32_t)lroundf(sum);
     h->geom = *g;
