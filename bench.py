@@ -258,7 +258,7 @@ def run_ours(args):
     P = wl.numsx * wl.numsy
     # the launch shape from the project's autotuner (cached per shape), as a
     # caller would run it; tuning happens before and outside the timed steps
-    tuned = h.autotune(epi, 256, Path(tempfile.gettempdir()) / f"ebsd_autotune_{local}.txt")
+    tuned = h.autotune(epi, 1024, Path(tempfile.gettempdir()) / f"ebsd_autotune_{local}.txt")
 
     # a dedicated stream: its handle is never 0, which the C ABI reads as
     # "the handle's own stream"; the events below are recorded on it
@@ -504,7 +504,7 @@ def run_c4(args):
     pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
     epi = capi.epilogue(pref)
     nx, ny = h.output_dims(epi)
-    tuned = h.autotune(epi, 256, Path(tempfile.gettempdir()) / "ebsd_autotune_0.txt")
+    tuned = h.autotune(epi, 1024, Path(tempfile.gettempdir()) / "ebsd_autotune_0.txt")
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     h.set_stream(stream.cuda_stream)
