@@ -611,12 +611,20 @@ def run_batched(args):
     def batched():
         runner.forward_batched(jobs, graph=True)
 
+    queue_runner = capi.Handle(0)
+    queue_runner.set_stream(stream.cuda_stream)
+
+    def queued():
+        queue_runner.forward_batched(jobs, graph=True, queue_all=True)
+
     def one_by_one():
         for h, q, epi, out in jobs:
             h.forward(q, epi, out=out)
 
     ms_b = timed(batched, args.steps)
     ref = [out.clone() for *_, out in jobs]
+    ms_q = timed(queued, args.steps)
+    same_q = all(torch.equal(r, out) for r, (*_, out) in zip(ref, jobs))
     ms_s = timed(one_by_one, args.steps)
     same = all(torch.equal(r, out) for r, (*_, out) in zip(ref, jobs))
     line = {
@@ -630,6 +638,9 @@ def run_batched(args):
                              "launches, the rest through one persistent queue kernel"},
         "one_by_one": {"value": total / (ms_s / 1e3), "ms_per_step": ms_s,
                        "launches": len(jobs)},
+        "persistent_only": {"value": total / (ms_q / 1e3), "ms_per_step": ms_q,
+                            "identical": bool(same_q),
+                            "what": "every job through the persistent queue kernel"},
         "identical_to_one_by_one": bool(same),
         "setup_s": setup_s,
     }

@@ -51,6 +51,7 @@ class Job(C.Structure):
 
 
 BATCH_GRAPH = 1
+BATCH_QUEUE_ALL = 2
 
 
 class GNOptions(C.Structure):
@@ -333,15 +334,17 @@ class Handle:
                                    C.byref(ty), C.byref(oc), C.byref(us)), self._h)
         return ty.value, oc.value, us.value
 
-    def forward_batched(self, jobs, graph: bool = False):
+    def forward_batched(self, jobs, graph: bool = False, queue_all: bool = False):
         """jobs: list of (source Handle, device quats tensor, Epilogue, device
-        out tensor).  Queued on this handle's stream."""
+        out tensor).  Queued on this handle's stream.  queue_all: every job
+        through the persistent queue kernel (default: jobs that fill the GPU
+        by themselves run as their own launches)."""
         arr = (Job * max(1, len(jobs)))()
         for i, (src, q, epi, out) in enumerate(jobs):
             arr[i] = Job(src.raw.value if hasattr(src.raw, "value") else src.raw, _ptr(q),
                          int(q.shape[0]), epi, _ptr(out))
-        _check(lib().ebsd_forward_batched(self._h, arr, len(jobs), BATCH_GRAPH if graph else 0),
-               self._h)
+        flags = (BATCH_GRAPH if graph else 0) | (BATCH_QUEUE_ALL if queue_all else 0)
+        _check(lib().ebsd_forward_batched(self._h, arr, len(jobs), flags), self._h)
 
     def gn_accumulate(self, quats, epi: Epilogue, targets, damping=1e-3, pc_system=False,
                       loss=None):

@@ -1267,7 +1267,8 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         b.p.quats = (const float4*)J.quats;
         b.p.out = J.out;
         b.p.n = J.n;
-        if (forward_ctas(b.p, src->cfg) >= (int64_t)kBatchLargeCtasPerSm * sms) {
+        if (!(flags & EBSD_BATCH_QUEUE_ALL) &&
+            forward_ctas(b.p, src->cfg) >= (int64_t)kBatchLargeCtasPerSm * sms) {
             BatchLarge L;
             memset(&L, 0, sizeof L);
             L.p = b.p;

@@ -301,9 +301,14 @@ __global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y
 // atomic increment and stops when the queue is exhausted -- no CTA waits
 // on another, so nothing can spin.  Jobs are ordered by item_begin.
 // TY is the tile height (CTA = 32 x TY threads); a group's jobs all use it.
-// Both heights get 1024 resident threads per SM at up to 64 registers.
+// Both heights get 1024 resident threads per SM at up to 64 registers
+// (EBSD_BATCH_MIN_BLOCKS4: resident 32 x 4 CTAs the register budget allows).
+#ifndef EBSD_BATCH_MIN_BLOCKS4
+#define EBSD_BATCH_MIN_BLOCKS4 8
+#endif
 template <int NV, bool NOISE, int TY>
-__global__ void __launch_bounds__(32 * TY, 32 / TY) k_forward_batched(const BatchJob* __restrict__ jobs,
+__global__ void __launch_bounds__(32 * TY, TY == 4 ? EBSD_BATCH_MIN_BLOCKS4 : 32 / TY)
+    k_forward_batched(const BatchJob* __restrict__ jobs,
                                                              const BatchHeader* __restrict__ hdr,
                                                              unsigned long long* __restrict__ counter)
 {

@@ -181,6 +181,7 @@ typedef struct {
 } ebsd_job;
 
 #define EBSD_BATCH_GRAPH 1 /* capture the batch in a CUDA graph and replay it */
+#define EBSD_BATCH_QUEUE_ALL 2 /* every job through the persistent queue kernel */
 
 /* Launch-shape autotuner (no reference counterpart): times the pattern
  * kernel for this handle's detector and epilogue over n_sample orientations
@@ -201,7 +202,8 @@ int ebsd_autotune(ebsd_handle* h, const ebsd_epilogue* e, int64_t n_sample,
  * handle's launch shape, e.g. the autotuner's) runs as that launch; the
  * others share a device work queue of (job, 32 x 4 or 32 x 8-pixel tile,
  * run of orientations) items consumed by a persistent grid (one launch per
- * energy-bin count, noise and tile height).  With EBSD_BATCH_GRAPH all of it
+ * energy-bin count, noise and tile height); EBSD_BATCH_QUEUE_ALL puts every
+ * job in the queue.  With EBSD_BATCH_GRAPH all of it
  * (table upload, queue reset, launches) is captured in a CUDA graph on first
  * use and replayed for later batches with the same queue shape and the same
  * large-job parameters.  Runs on h's stream; returns when the work is

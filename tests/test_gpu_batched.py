@@ -179,3 +179,8 @@ def test_batched_large_jobs_run_as_own_launches(built):
     jobs[3] = (h, q, epi, torch.full_like(out, -1.0))
     runner.forward_batched(jobs, graph=True)
     check("new buffer")
+    # every job through the queue kernel: the same records
+    for h, q, epi, out in jobs:
+        out.fill_(-1.0)
+    capi.Handle(0).forward_batched(jobs, graph=True, queue_all=True)
+    check("queue only")
