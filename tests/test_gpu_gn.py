@@ -26,8 +26,9 @@ def perturb(q, sigma_deg, rng):
     return out.astype(np.float32)
 
 
-def _problem(torch, binning=1, n=64, pc_shift=(0.0, 0.0, 0.0)):
-    wl = synth.tiny(seed=4, numsx=96, numsy=80, npx=120, nE=5, mc_nsx=150, n_orient=n)
+def _problem(torch, binning=1, n=64, pc_shift=(0.0, 0.0, 0.0), size=(96, 80)):
+    wl = synth.tiny(seed=4, numsx=size[0], numsy=size[1], npx=120, nE=5, mc_nsx=150,
+                    n_orient=n)
     wl.delta = 100.0
     wl.mc_total = 4e6
     sr, acc = wl.master(), wl.mc()
@@ -63,6 +64,19 @@ def test_refine_orientations(built, binning):
     print("binning", binning, "iterations", it, "max misorientation (deg)", mis.max())
     assert mis.max() < 0.01
     assert loss.max().item() < 1e-6
+
+
+@pytest.mark.parametrize("binning", [1, 2, 4])
+def test_refine_on_a_ragged_detector(built, binning):
+    """99 x 75 pixels: partial tiles, and binning blocks cropped to the floor."""
+    torch = pytest.importorskip("torch")
+    wl, h, epi, qt, targets, _ = _problem(torch, binning, n=32, size=(99, 75))
+    rng = np.random.default_rng(2)
+    dq = torch.from_numpy(perturb(qt, 1.0, rng)).cuda()
+    it, _ = h.refine(dq, epi, targets, max_iterations=20, damping=1e-4, tol_rad=1e-7)
+    mis = misorientation_deg(dq.cpu().numpy(), qt)
+    print("binning", binning, "iterations", it, "max misorientation (deg)", mis.max())
+    assert mis.max() < 0.01
 
 
 def test_refine_orientations_and_centre(built):

@@ -69,6 +69,26 @@ def test_ndp_matches_fp64_analytic(built, binning):
     h.close()
 
 
+@pytest.mark.parametrize("binning", [1, 2, 4])
+def test_ragged_detector_matches_fp64_analytic(built, binning):
+    """A detector whose sides are not multiples of the tile (70 x 45): partial
+    tiles, and binning blocks cropped to the floor (CTEMEBSD.f90:630-651)."""
+    from oracle import oracle as O
+    wl = synth.tiny(seed=5, numsx=70, numsy=45, npx=60, nE=5, mc_nsx=80, n_orient=6)
+    wl.delta = 110.0
+    sr, acc = wl.master(), wl.mc()
+    q = wl.quaternions()
+    h, pref = _handle(wl, sr, acc)
+    T = _targets(O, wl, sr, acc, q, binning)
+    mode = "lin" if binning > 1 else "not"
+    loss, g = h.vjp(q, capi.epilogue(pref, binning=binning, scalingmode=mode), T, "ndp")
+    rloss, rg = O.vjp_f64(wl.geometry(), acc, 1, wl.nEbins, sr, q, pref, binning, "ndp", T)
+    np.testing.assert_allclose(loss, rloss, rtol=1e-3, atol=1e-6)
+    err = _grad_err(g, rg)
+    assert (err < TOL_GRAD).all(), err
+    h.close()
+
+
 def test_cotangent_matches_fp64_analytic(built):
     from oracle import oracle as O
     wl = _wl()
