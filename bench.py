@@ -428,10 +428,19 @@ def _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, fwd_value)
         tot = float(t.item())
     v = world * N * args.vjp_steps / (tot / 1000.0)
     lh = loss.cpu().numpy()
+    # algorithmic bytes: the recomputed 4-corner gather twice over (value and
+    # slopes share it, the weight terms read it again per bin) + the target
+    # read and the per-pattern outputs: P (2 x 16 nE + 8)
+    b_vjp = wl.numsx * wl.numsy * (2 * 16 * wl.nEbins + 8)
+    peak, peak_kind = _peaks()
+    ach = b_vjp * (v / world) / 1e9
     return {"value": v, "unit": UNIT, "ratio_to_forward": v / fwd_value,
             "ms_per_step": tot / args.vjp_steps, "steps": args.vjp_steps,
             "what": "loss 1 - normalised dot product + gradient w.r.t. 3 rotation tangents "
                     "and (xpc, ypc, L), one fused pass per pattern",
+            "roofline": {"algorithmic_bytes_per_pattern": b_vjp, "achieved": ach,
+                         "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "peak_kind": peak_kind},
             "mean_loss": float(lh.mean()), "finite": bool(np.isfinite(lh).all())}
 
 
@@ -539,6 +548,8 @@ def run_c4(args):
         "forward": {"value": fwd, "unit": UNIT, "steps": args.steps,
                     "launch_shape": {"tile_y": tuned[0], "orient_per_cta": tuned[1]}},
         "ratio_to_forward": vjp["ratio_to_forward"], "what": vjp["what"],
+        "roofline": dict(vjp["roofline"], bound="hbm",
+                         note="algorithmic bytes of the recomputed gather; served by L1/L2"),
         "mean_loss": vjp["mean_loss"], "finite": vjp["finite"],
         "gpu_launches": 2 * args.vjp_steps, "clocks": ck,
     }

@@ -90,7 +90,8 @@ struct ebsd_handle {
     int mc_fp32 = 0;     // Monte-Carlo trajectories in binary32
     int host_direct = 1; // kernel stores straight into pinned host outputs
     int vjp_tile_y = 4;  // adjoint / Gauss-Newton CTA height (8 for binning 8)
-    int vjp_opc = 8;     // adjoint / Gauss-Newton orientations per CTA
+    int vjp_opc = 8;     // adjoint orientations per CTA
+    int gn_opc = 32;     // Gauss-Newton orientations per CTA
     int weights_fp64 = 1;
     int lambert_accurate = 0;
 
@@ -416,6 +417,10 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
         if (value != 4 && value != 8)
             return set_err(h, EBSD_EINVAL, "vjp_tile_y must be 4 or 8");
         h->vjp_tile_y = (int)value;
+    } else if (k == "gn_orient_per_cta") {
+        if (value < 1 || value > 64)
+            return set_err(h, EBSD_EINVAL, "gn_orient_per_cta must be in 1..64");
+        h->gn_opc = (int)value;
     } else if (k == "vjp_orient_per_cta") {
         if (value < 1 || value > 64)
             return set_err(h, EBSD_EINVAL, "vjp_orient_per_cta must be in 1..64");
@@ -1064,7 +1069,7 @@ extern "C" int ebsd_gn_accumulate(ebsd_handle* h, const float* quats, int64_t n,
     vp.drg = h->d_drg;
     vp.dW = h->d_dW;
     vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
-    vp.opc = h->vjp_opc;
+    vp.opc = h->gn_opc;
     const int tile_y = vp.binning > h->vjp_tile_y ? 8 : h->vjp_tile_y;
     if (vp.binning > tile_y)
         return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: binning %d exceeds the tile",

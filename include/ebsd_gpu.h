@@ -114,9 +114,11 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    per SM.
  *   "vjp_tile_y"     CTA height of ebsd_vjp and the Gauss-Newton kernels:
  *                    4 (default) or 8; binning 8 always uses 8.
- *   "vjp_orient_per_cta"  their orientations per CTA, 1..64 (default 8).
+ *   "vjp_orient_per_cta"  ebsd_vjp's orientations per CTA, 1..64 (default 8).
  *                    (ebsd_vjp_noalloc keeps 8 and 2, the shape its size
  *                    limit is stated for.)
+ *   "gn_orient_per_cta"   the Gauss-Newton kernels', 1..64 (default 32: 3 %
+ *                    faster refinement at 120x120 than 8).
  *   "host_direct"    1 (default): for a pinned host destination the pattern
  *                    kernel stores the records straight into it through its
  *                    mapped address (157 k patterns/s end to end at 640x480
