@@ -14,6 +14,7 @@ module ebsd_gpu
                                EBSD_EFORMAT = -6, EBSD_EUNSUPPORTED = -7, EBSD_ETIMEOUT = -8
   integer(c_int32_t), parameter :: EBSD_SCALING_NOT = 0, EBSD_SCALING_LIN = 1, &
                                    EBSD_SCALING_GAM = 2
+  integer(c_int32_t), parameter :: EBSD_VJP_COTANGENT = 0, EBSD_VJP_NDP = 1
 
   type, bind(C) :: ebsd_geometry
     real(c_float)     :: L, thetac, delta
@@ -29,6 +30,11 @@ module ebsd_gpu
     integer(c_int32_t):: poisson
     integer(c_int64_t):: seed
   end type ebsd_epilogue
+
+  type, bind(C) :: ebsd_gn_options
+    integer(c_int32_t):: max_iterations, refine_pc
+    real(c_double)    :: damping, tol_rad, tol_pc
+  end type ebsd_gn_options
 
   interface
     integer(c_int) function ebsd_create(h, device) bind(C, name="ebsd_create")
@@ -115,6 +121,53 @@ module ebsd_gpu
       import :: c_int, c_char
       character(kind=c_char), intent(in) :: nmlfile(*)  ! NUL-terminated
       integer(c_int), value :: device, quiet
+    end function
+
+    ! The CTEMMC program (&MCdata namelist in, MC file out).
+    integer(c_int) function ebsd_run_mc_namelist(nmlfile, device, quiet) &
+        bind(C, name="ebsd_run_mc_namelist")
+      import :: c_int, c_char
+      character(kind=c_char), intent(in) :: nmlfile(*)  ! NUL-terminated
+      integer(c_int), value :: device, quiet
+    end function
+
+    ! Tuning and precision options by name, e.g. "strict_order"//c_null_char.
+    integer(c_int) function ebsd_set_option(h, key, val) bind(C, name="ebsd_set_option")
+      import :: c_int, c_ptr, c_char, c_int64_t
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(in) :: key(*)      ! NUL-terminated
+      integer(c_int64_t), value :: val
+    end function
+
+    ! Adjoint: gradient of the records (or of the loss against target records,
+    ! mode EBSD_VJP_NDP) with respect to the 3 rotation tangents and (xpc, ypc, L).
+    integer(c_int) function ebsd_vjp(h, quats, n, e, mode, data, loss, grad) &
+        bind(C, name="ebsd_vjp")
+      import :: c_int, c_ptr, c_float, c_int32_t, c_int64_t, ebsd_epilogue
+      type(c_ptr), value :: h
+      real(c_float), intent(in) :: quats(*)        ! quatang(4,n)
+      integer(c_int64_t), value :: n
+      type(ebsd_epilogue), intent(in) :: e
+      integer(c_int32_t), value :: mode
+      real(c_float), intent(in) :: data(*)         ! n records of (nx,ny)
+      real(c_float), intent(out) :: loss(*)        ! loss(n), mode EBSD_VJP_NDP
+      real(c_float), intent(out) :: grad(*)        ! grad(6,n)
+    end function
+
+    ! Gauss-Newton refinement; quats, targets and loss are device pointers.
+    integer(c_int) function ebsd_refine(h, quats, n, e, targets, opt, loss, geom, iterations) &
+        bind(C, name="ebsd_refine")
+      import :: c_int, c_ptr, c_int32_t, c_int64_t, ebsd_epilogue, ebsd_gn_options, &
+                ebsd_geometry
+      type(c_ptr), value :: h
+      type(c_ptr), value :: quats                   ! device float(4,n), updated in place
+      integer(c_int64_t), value :: n
+      type(ebsd_epilogue), intent(in) :: e
+      type(c_ptr), value :: targets                 ! device, n records
+      type(ebsd_gn_options), intent(in) :: opt
+      type(c_ptr), value :: loss                    ! device float(n) or c_null_ptr
+      type(ebsd_geometry), intent(inout) :: geom
+      integer(c_int32_t), intent(out) :: iterations
     end function
   end interface
 

@@ -79,3 +79,22 @@ def test_cli_help_and_template(built, tmp_path):
     r = subprocess.run([str(exe), str(tmp_path / "missing.nml")], capture_output=True,
                        text=True, cwd=tmp_path)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+def test_fortran_module_binds_declared_functions():
+    """Every bind(C, name=...) of the Fortran module names a function the C
+    header declares, and the module's derived types mirror the C structs
+    field by field."""
+    src = (ROOT / "ctemsoft_gb300" / "fortran" / "ebsd_gpu.f90").read_text()
+    bound = re.findall(r'bind\(C,\s*name="(ebsd_[a-z0-9_]+)"\)', src)
+    assert bound and set(bound) <= set(declared_functions()), set(bound) - set(declared_functions())
+    header = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "ebsd_gpu.h").read_text(), flags=re.S)
+    for name in ("ebsd_geometry", "ebsd_epilogue", "ebsd_gn_options"):
+        c_body = re.search(r"typedef struct \{([^{}]*)\}\s*" + name + ";", header).group(1)
+        c_fields = [f.strip().split()[-1] for decl in c_body.split(";") if decl.strip()
+                    for f in decl.split(",")]
+        f_body = re.search(r"type, bind\(C\) :: " + name + r"(.*?)end type", src, re.S).group(1)
+        f_fields = [f.strip() for line in f_body.strip().splitlines()
+                    for f in line.split("::")[1].split("!")[0].split(",")]
+        assert [f.lower() for f in f_fields] == [f.lower() for f in c_fields], (name, f_fields,
+                                                                                 c_fields)
