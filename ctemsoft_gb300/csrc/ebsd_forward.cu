@@ -263,13 +263,20 @@ constexpr int kAutoOpc = 64, kAutoMinCtasPerSm = 32;
 int resolve_opc(int opc, int64_t n, int ntiles)
 {
     if (opc > 0) return opc;
-    static int sms = 0;
+    // SM count of the current device, looked up once per device (a benign
+    // race: every thread that looks it up stores the same value)
+    constexpr int kMaxDevices = 64;
+    static int sms_of[kMaxDevices] = {};
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < kMaxDevices) sms = sms_of[dev];
     if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            sms < 1)
+            sms < 1) {
+            cudaGetLastError();
             sms = 1;
+        }
+        if (dev >= 0 && dev < kMaxDevices) sms_of[dev] = sms;
     }
     int o = kAutoOpc;
     while (o > 1 && ((n + o - 1) / o) * (int64_t)ntiles < (int64_t)kAutoMinCtasPerSm * sms) o >>= 1;
