@@ -233,3 +233,24 @@ def test_epilogue(O):
     np.testing.assert_allclose(g, pat.astype(np.float64) ** 0.33, rtol=1e-6)
     n = O.epilogue_f32(pat, 8, 0, 0.33)  # 'not': untouched, full size
     assert np.array_equal(n, pat)
+
+
+@pytest.mark.parametrize("b", [2, 4, 8])
+def test_epilogue_reference_order_is_bit_exact(O, b):
+    """The restated block sum of CTEMEBSD.f90:636-640 in single precision:
+    one addition at a time, x fastest within the block, then times 1/b^2 --
+    checked bit for bit against the same order written independently here."""
+    rng = np.random.default_rng(10 + b)
+    ny, nx = 5 * b + 3, 7 * b + 5                  # ragged: crop to whole blocks
+    pat = rng.uniform(0.1, 3.0, size=(ny, nx)).astype(np.float32)
+    got = O.epilogue_f32(pat, b, 1, 1.0)
+    bindx = np.float32(1.0) / (np.float32(b) * np.float32(b))
+    ref = np.empty((ny // b, nx // b), np.float32)
+    for J in range(ny // b):
+        for I in range(nx // b):
+            s = np.float32(0.0)
+            for jj in range(b):
+                for ii in range(b):
+                    s = np.float32(s + pat[J * b + jj, I * b + ii])
+            ref[J, I] = np.float32(s * bindx)
+    assert np.array_equal(got, ref)
