@@ -98,3 +98,17 @@ def test_fortran_module_binds_declared_functions():
                     for f in line.split("::")[1].split("!")[0].split(",")]
         assert [f.lower() for f in f_fields] == [f.lower() for f in c_fields], (name, f_fields,
                                                                                  c_fields)
+
+
+def test_every_option_key_is_documented():
+    """Each key ebsd_set_option accepts is described in the header, and an
+    unknown key is rejected by name."""
+    src = (ROOT / "ctemsoft_gb300" / "csrc" / "ebsd_capi.cu").read_text()
+    body = src[src.index('extern "C" int ebsd_set_option'):]
+    body = body[:body.index("\n}\n")]
+    keys = sorted(set(re.findall(r'k == "([a-z0-9_]+)"', body)))
+    assert "l2_persist" in keys and "orient_per_cta" in keys
+    header = (ROOT / "include" / "ebsd_gpu.h").read_text()
+    missing = [k for k in keys if f'"{k}"' not in header]
+    assert not missing, missing
+    assert "unknown option" in body
