@@ -254,3 +254,46 @@ def test_epilogue_reference_order_is_bit_exact(O, b):
                     s = np.float32(s + pat[J * b + jj, I * b + ii])
             ref[J, I] = np.float32(s * bindx)
     assert np.array_equal(got, ref)
+
+
+def test_gradient_oracle_matches_its_finite_differences(O):
+    """The analytic binary64 gradient (the adjoint's checker) against central
+    binary64 finite differences of the oracle's own forward: loss 1 - the
+    normalised dot product with targets, h = 1e-4 rad, 1e-3 px, 1e-2 um, the
+    detector re-evaluated for every pattern-centre step.  The bilinear
+    interpolation has kinks at cell edges, which the differences average
+    over, hence 2e-2 relative to the largest component of each kind."""
+    wl = synth.tiny(seed=5, numsx=40, numsy=30, npx=60, nE=5, mc_nsx=80, n_orient=3)
+    wl.delta = 120.0
+    sr, acc = wl.master(), wl.mc()
+    qd = wl.quaternions(3).astype(np.float64)
+    geom = dict(wl.geometry(), exact=True)
+    det = O.Detector(geom, acc, 1, wl.nEbins)
+    qt = np.stack([O.rotate_left(x, np.radians([0.4, -0.3, 0.2])) for x in qd])
+    T = det.patterns_f64(sr, qt, 1.0).astype(np.float32)
+
+    def L(gm, qs):
+        P = O.Detector(gm, acc, 1, wl.nEbins).patterns_f64(sr, qs, 1.0)
+        Td = T.astype(np.float64)
+        return np.array([1 - (p * t).sum() / np.sqrt((p * p).sum() * (t * t).sum())
+                         for p, t in zip(P, Td)])
+
+    loss, g = O.vjp_f64(geom, acc, 1, wl.nEbins, sr, qd, 1.0, 1, "ndp", T, nthreads=1)
+    np.testing.assert_allclose(loss, L(geom, qd), rtol=1e-12, atol=1e-15)
+    fd = np.zeros((len(qd), 6))
+    for a in range(3):
+        w = np.zeros(3)
+        w[a] = 1e-4
+        qp = np.stack([O.rotate_left(x, w) for x in qd])
+        qm = np.stack([O.rotate_left(x, -w) for x in qd])
+        fd[:, a] = (L(geom, qp) - L(geom, qm)) / 2e-4
+    for a, (k, st) in enumerate((("xpc", 1e-3), ("ypc", 1e-3), ("L", 1e-2))):
+        gp, gm = dict(geom), dict(geom)
+        gp[k] += st
+        gm[k] -= st
+        fd[:, 3 + a] = (L(gp, qd) - L(gm, qd)) / (2 * st)
+    for cols in ((0, 1, 2), (3,), (4,), (5,)):
+        scale = np.abs(fd[:, cols]).max()
+        assert scale > 0
+        err = np.abs(g[:, cols] - fd[:, cols]).max() / scale
+        assert err < 2e-2, (cols, err)
