@@ -106,6 +106,7 @@ int64_t oracle_mc_philox(const oracle_mc_params* p, uint64_t seed, int64_t e0, i
 int64_t oracle_mc_reference_rng(const oracle_mc_params* p, int32_t primeseed, int nthreads,
                                 int64_t num_el, int32_t* accum_e, int32_t* accum_z);
 void oracle_mc_uniforms(int kind, uint64_t seed_or_prime, int64_t electron, int count, float* u);
+void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 #ifdef __cplusplus
 }

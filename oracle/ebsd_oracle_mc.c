@@ -104,6 +104,15 @@ static void philox(uint32_t c[4], uint32_t k0, uint32_t k1)
     }
 }
 
+/* One raw Philox4x32-10 block, exported so that the generator can be checked
+ * against the published known-answer vectors of its authors. */
+void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    philox(c, key[0], key[1]);
+    for (int i = 0; i < 4; ++i) out[i] = c[i];
+}
+
 typedef struct {
     int kind;  /* 0 Philox, 1 reference */
     /* Philox */

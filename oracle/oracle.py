@@ -82,6 +82,7 @@ _SIGS = {
     "oracle_mc_philox": (C.c_int64, [_P, C.c_uint64, C.c_int64, C.c_int64, _P, _P]),
     "oracle_mc_reference_rng": (C.c_int64, [_P, C.c_int32, C.c_int, C.c_int64, _P, _P]),
     "oracle_mc_uniforms": (None, [C.c_int, C.c_uint64, C.c_int64, C.c_int, _P]),
+    "oracle_philox4x32_10": (None, [_P, _P, _P]),
 }
 
 _lib = None
@@ -443,3 +444,12 @@ def mc_uniforms(kind: int, seed: int, electron: int, count: int):
     u = np.zeros(count, np.float32)
     lib().oracle_mc_uniforms(kind, seed, electron, count, _p(u))
     return u
+
+
+def philox4x32_10(ctr, key):
+    """One Philox4x32-10 block: four 32-bit counter words, two key words."""
+    c = np.ascontiguousarray(ctr, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib().oracle_philox4x32_10(_p(c), _p(k), _p(out))
+    return out

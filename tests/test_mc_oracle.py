@@ -85,3 +85,15 @@ def test_out_of_range_parameters():
         O.mc_dims(O.mc_params(numsx=100))
     with pytest.raises(ValueError):
         O.mc_dims(O.mc_params(EkeV=5.0, Ehistmin=10.0))
+
+
+@pytest.mark.parametrize("ctr,key,want", [
+    ((0, 0, 0, 0), (0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+    ((0xffffffff,) * 4, (0xffffffff,) * 2, (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+    ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+     (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1)),
+])
+def test_philox_known_answers(ctr, key, want):
+    """Philox4x32-10 against the known-answer vectors its authors publish
+    with the generator (Salmon et al., SC'11; counter, key -> block)."""
+    assert O.philox4x32_10(ctr, key).tolist() == list(want)
