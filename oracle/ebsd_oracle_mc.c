@@ -3,7 +3,8 @@
  * histogram (CTEMMC.f90:307-529, single_run; CSDA mode).
  * TEST INFRASTRUCTURE ONLY (the checker for ebsd_mc_run).
  * PARITY UNPINNED: the reference has no tests or fixtures for CTEMMC and
- * cannot be compiled here.
+ * cannot be compiled here.  (The Philox4x32-10 block below is pinned to the
+ * known-answer vectors its authors publish; the trajectory physics is not.)
  *
  * Two random-number sources drive the same trajectory code:
  *   - the GPU's: Philox4x32-10 keyed by the seed, counter (draw/4, 0,
