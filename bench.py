@@ -66,6 +66,11 @@ def _args():
     ap.add_argument("--dict-steps", type=int, default=100,
                     help="dict: cubochoric steps per semi-edge of the m-3m zone")
     ap.add_argument("--fd-iters", type=int, default=3)
+    ap.add_argument("--legs", default="c3,c4,c5",
+                    help="workloads added to the default line as sub-objects (comma list of "
+                         "c3, c4, c5; empty for none)")
+    ap.add_argument("--legs-fd-iters", type=int, default=2,
+                    help="c5 leg of the default line: finite-difference baseline iterations")
     return ap.parse_args()
 
 
@@ -77,24 +82,63 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _traffic_per_pattern():
-    """DRAM bytes per pattern of the pattern kernel from the committed ncu
-    summary (profiles/), or None."""
+def _ncu_summary(key: str):
+    """A figure of the pattern kernel's committed ncu summary (profiles/),
+    written there as `key = value`, or None."""
     f = ROOT / "profiles" / "k_forward_640x480.md"
     if not f.exists():
         return None
-    m = re.search(r"traffic_bytes_per_pattern\s*=\s*([0-9.eE+]+)", f.read_text())
+    m = re.search(re.escape(key) + r"\s*=\s*([0-9.eE+]+)", f.read_text())
     return float(m.group(1)) if m else None
 
 
-def _l1_wavefront_frac():
-    """The pattern kernel's L1 data-pipe wavefront rate (fraction of peak)
-    from the committed ncu summary, or None."""
-    f = ROOT / "profiles" / "k_forward_640x480.md"
-    if not f.exists():
-        return None
-    m = re.search(r"L1 data-pipe wavefronts \(LSU\) \| ([0-9.]+) %", f.read_text())
-    return float(m.group(1)) / 100.0 if m else None
+def _cache_peaks(device: int):
+    """Read bandwidth of L1 (hits, 128-bit loads), of L2 (a 48 MB resident
+    working set, the interleaved master's size, L1 bypassed) and of HBM (a
+    2 GiB sweep), measured now on this device (GB/s)."""
+    from ctemsoft_gb300 import capi
+    return {"l1": capi.measure_bandwidth(device, capi.BW_L1, 16, 5),
+            "l2": capi.measure_bandwidth(device, capi.BW_L2, 48 << 20, 5),
+            "hbm_read": capi.measure_bandwidth(device, capi.BW_HBM, 2 << 30, 3)}
+
+
+def _roofline(b_pattern: int, n: int, launch_ms: float, peaks: dict) -> dict:
+    """The pattern kernel against the memory level that bounds it.  Its
+    algorithmic bytes (4 corners x nE master values + one store per pixel)
+    all pass through the L1 data pipe (82 % L1 hits at 640x480: neighbouring
+    pixels share master nodes), so the measured L1 read rate is the roof;
+    the L2 and HBM figures are the lower levels' share of the same bytes."""
+    hbm_copy, hbm_kind = _peaks()
+    achieved = b_pattern * n / (launch_ms / 1000.0) / 1e9
+    l1, l2 = peaks["l1"], peaks["l2"]
+    dram_pp = _ncu_summary("traffic_bytes_per_pattern")
+    l2_pp = _ncu_summary("l2_bytes_per_pattern")
+    frac = achieved / l1
+    return {
+        "bound": "l1", "achieved": achieved, "peak": l1, "unit": "GB/s", "frac": frac,
+        "peak_kind": "measured in this run: L1-hit 128-bit loads (ebsd_measure_bandwidth)",
+        "traffic": (dram_pp * n if dram_pp else None),
+        "traffic_source": "ncu capture of one 256-orientation launch at 640x480 "
+                          "(dram__bytes_read.sum + dram__bytes_write.sum), scaled by the "
+                          "pattern count; profiles/k_forward_640x480.md",
+        "algorithmic_bytes_per_pattern": b_pattern,
+        "target": {"what": ">= 60 % of the gather roofline", "frac": frac,
+                   "met": bool(frac >= 0.6), "level": "l1"},
+        "levels": {
+            "l1": {"peak": l1, "frac": frac},
+            "l2": {"peak": l2, "frac_if_all_bytes_from_l2": achieved / l2,
+                   "l2_bytes_per_pattern": l2_pp,
+                   "frac_of_l2_peak": (l2_pp * n / (launch_ms / 1000.0) / 1e9 / l2
+                                       if l2_pp else None),
+                   "l2_bytes_source": "ncu lts__t_bytes of the same capture"},
+            "hbm": {"peak_copy": hbm_copy, "peak_copy_kind": hbm_kind,
+                    "peak_read_sweep": peaks["hbm_read"],
+                    "frac_of_copy_if_all_bytes_from_hbm": achieved / hbm_copy},
+        },
+        "binding_unit": {"unit": "L1 data pipe (LSU wavefronts)",
+                         "frac": _ncu_summary("l1_wavefront_frac"),
+                         "source": "profiles/k_forward_640x480.md"},
+    }
 
 
 class Clocks:
@@ -296,13 +340,15 @@ def run_ours(args):
         tot_ms = float(t.item())
     value = world * N * args.steps / (tot_ms / 1000.0)
     launch_ms = statistics.mean(step_ms)
+    peaks = _cache_peaks(local)
 
     # fused forward + adjoint: the normalised-dot-product loss and its
     # gradient (3 rotation tangents + pattern centre) for every orientation
     # against target patterns, one pass per pattern
     fwd_vjp = None
     if args.vjp_steps > 0:
-        fwd_vjp = _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, value)
+        fwd_vjp = _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, value,
+                           flush, peaks)
 
     # the same loop with the reference's Poisson noise (CTEMEBSD.f90:611-615)
     # before the gamma epilogue
@@ -346,15 +392,33 @@ def run_ours(args):
     if args.e2e_steps > 0:
         e2e = _e2e(h, q, epi, N, nx, ny, args, world, dev, barrier)
 
+    # the other workloads, one compact sub-object each (rank 0 of a 1-GPU run)
+    legs = {}
+    if rank == 0 and world == 1 and args.legs:
+        h.close()
+        h = None
+        del dq
+        torch.cuda.empty_cache()
+        for name in [x.strip() for x in args.legs.split(",") if x.strip()]:
+            try:
+                if name == "c3":
+                    legs["c3"] = c3_measure(args, 3)
+                elif name == "c4":
+                    legs["c4"] = c4_measure(args, 5, 3)
+                elif name == "c5":
+                    legs["c5"] = c5_measure(args, args.legs_fd_iters)
+                    legs["c5"]["fd_note"] = (f"forward-only finite-difference baseline capped "
+                                             f"at {args.legs_fd_iters} iterations")
+            except Exception as ex:  # a failed leg is reported, the headline stands
+                legs[name] = {"error": f"{type(ex).__name__}: {ex}"}
+            torch.cuda.empty_cache()
+
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(wl, sr, acc, q, args.cpu_seconds)
 
     if rank == 0:
-        peak, peak_kind = _peaks()
         b_pattern = P * (16 * wl.nEbins + 4)
-        achieved = b_pattern * N / (launch_ms / 1000.0) / 1e9
-        tpp = _traffic_per_pattern()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_ms / args.steps,
@@ -367,15 +431,7 @@ def run_ours(args):
                        "parallelism": f"orientation shards x{world}",
                        "launch_shape": {"tile_y": tuned[0], "orient_per_cta": tuned[1],
                                         "source": "ebsd_autotune"}},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": (tpp * N if tpp else None),
-                         "algorithmic_bytes_per_pattern": b_pattern,
-                         "note": "gathered master bytes are served by L1/L2 (master is "
-                                 "L2-resident), so frac can exceed 1",
-                         "binding_unit": {"unit": "L1 data pipe (LSU wavefronts)",
-                                          "frac": _l1_wavefront_frac(),
-                                          "source": "profiles/k_forward_640x480.md"}},
+            "roofline": _roofline(b_pattern, N, launch_ms, peaks),
             "e2e": e2e,
             "fwd_vjp": fwd_vjp,
             "fwd_noise": fwd_noise,
@@ -383,14 +439,17 @@ def run_ours(args):
             "clocks": ck,
             "cpu_baseline": base,
         }
+        line.update(legs)
         print(json.dumps(line))
-    h.close()
+    if h is not None:
+        h.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
 
 
-def _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, fwd_value):
+def _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, fwd_value, flush,
+             peaks=None):
     import numpy as np
     import torch
 
@@ -417,6 +476,7 @@ def _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, fwd_value)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.vjp_steps)]
     for k in range(args.vjp_steps):
+        flush.zero_()  # evict L2 between timed steps, as in the forward leg
         ev[k][0].record(stream)
         h.vjp(dq, epi, dout, "ndp", loss=loss, grad=grad)
         ev[k][1].record(stream)
@@ -432,15 +492,18 @@ def _fwd_vjp(h, q, wl, pref, dout, stream, args, world, dev, barrier, fwd_value)
     # slopes share it, the weight terms read it again per bin) + the target
     # read and the per-pattern outputs: P (2 x 16 nE + 8)
     b_vjp = wl.numsx * wl.numsy * (2 * 16 * wl.nEbins + 8)
-    peak, peak_kind = _peaks()
+    if peaks is None:
+        peaks = _cache_peaks(dev.index if dev.index is not None else 0)
+    peak = peaks["l1"]
     ach = b_vjp * (v / world) / 1e9
     return {"value": v, "unit": UNIT, "ratio_to_forward": v / fwd_value,
             "ms_per_step": tot / args.vjp_steps, "steps": args.vjp_steps,
+            "l2": "flushed (512 MB write) between timed steps",
             "what": "loss 1 - normalised dot product + gradient w.r.t. 3 rotation tangents "
                     "and (xpc, ypc, L), one fused pass per pattern",
-            "roofline": {"algorithmic_bytes_per_pattern": b_vjp, "achieved": ach,
-                         "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                         "peak_kind": peak_kind},
+            "roofline": {"bound": "l1", "algorithmic_bytes_per_pattern": b_vjp,
+                         "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                         "peak_kind": "measured in this run: L1-hit 128-bit loads"},
             "mean_loss": float(lh.mean()), "finite": bool(np.isfinite(lh).all())}
 
 
@@ -493,11 +556,11 @@ def _e2e(h, q, epi, N, nx, ny, args, world, dev, barrier):
                              "cudaMemcpy device-to-host into the same pinned memory"}}
 
 
-def run_c4(args):
+def c4_measure(args, steps: int, vjp_steps: int) -> dict:
     """The adjoint workload: 480x480 detector, 1001^2 x 11-bin master, 4096
     orientations; the fused forward + adjoint (loss and its gradient with
     respect to 3 rotation tangents and the pattern centre) against the plain
-    forward of the same patterns."""
+    forward of the same patterns, both timed with L2 flushed between steps."""
     import torch
 
     from ctemsoft_gb300 import capi, synth
@@ -523,10 +586,8 @@ def run_c4(args):
     for _ in range(args.warmup):
         h.forward(dq, epi, out=dout)
     torch.cuda.synchronize()
-    clocks = Clocks(0)
-    clocks.start()
     tot = 0.0
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
@@ -534,35 +595,47 @@ def run_c4(args):
         b.record(stream)
         torch.cuda.synchronize()
         tot += a.elapsed_time(b)
-    fwd = N * args.steps / (tot / 1000.0)
-    vjp = _fwd_vjp(h, q, wl, pref, dout, stream, args, 1, dev, torch.cuda.synchronize, fwd)
-    ck = clocks.stop()
-    line = {
-        "metric": "EBSD fused forward + adjoint patterns/s (480x480, 4096 orientations)",
-        "value": vjp["value"], "unit": UNIT, "n_gpus": 1, "steps": args.vjp_steps,
-        "warmup": args.warmup, "ms_per_step": vjp["ms_per_step"], "higher_is_better": True,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wl.name, "detector": f"{wl.numsx}x{wl.numsy}",
-                   "master": f"{2 * wl.npx + 1}^2 x {wl.nEbins} bins", "orientations": N,
-                   "l2": "flushed between the forward's timed steps"},
-        "forward": {"value": fwd, "unit": UNIT, "steps": args.steps,
-                    "launch_shape": {"tile_y": tuned[0], "orient_per_cta": tuned[1]}},
-        "ratio_to_forward": vjp["ratio_to_forward"], "what": vjp["what"],
-        "roofline": dict(vjp["roofline"], bound="hbm",
-                         note="algorithmic bytes of the recomputed gather; served by L1/L2"),
-        "mean_loss": vjp["mean_loss"], "finite": vjp["finite"],
-        "gpu_launches": 2 * args.vjp_steps, "clocks": ck,
-    }
-    print(json.dumps(line))
+    fwd = N * steps / (tot / 1000.0)
+    sub = argparse.Namespace(warmup=args.warmup, vjp_steps=vjp_steps)
+    vjp = _fwd_vjp(h, q, wl, pref, dout, stream, sub, 1, dev, torch.cuda.synchronize, fwd,
+                   flush)
+    torch.cuda.set_stream(torch.cuda.default_stream(dev))
     h.close()
+    return {
+        "metric": "EBSD fused forward + adjoint patterns/s (480x480, 4096 orientations)",
+        "value": vjp["value"], "unit": UNIT, "ms_per_step": vjp["ms_per_step"],
+        "steps": vjp_steps, "forward": {"value": fwd, "unit": UNIT, "steps": steps,
+                                        "launch_shape": {"tile_y": tuned[0],
+                                                         "orient_per_cta": tuned[1]}},
+        "ratio_to_forward": vjp["ratio_to_forward"], "what": vjp["what"],
+        "roofline": vjp["roofline"], "mean_loss": vjp["mean_loss"], "finite": vjp["finite"],
+        "l2": "flushed (512 MB write) between timed steps of both legs",
+    }
+
+
+def run_c4(args):
+    clocks = Clocks(0)
+    clocks.start()
+    res = c4_measure(args, args.steps, args.vjp_steps)
+    ck = clocks.stop()
+    line = dict(res, n_gpus=1, warmup=args.warmup, higher_is_better=True, dtype="f32",
+                data="synthetic", gpu_launches=2 * args.vjp_steps, clocks=ck,
+                config={"workload": "adjoint-480x480-npx500", "detector": "480x480",
+                        "master": "1001^2 x 11 bins", "orientations": 4096})
+    print(json.dumps(line))
     return 0
 
 
-def run_batched(args):
+def c3_measure(args, steps: int) -> dict:
     """The batched uneven workload: 64 jobs (seed 2) of mixed detector size,
-    binning, orientation count and phase in one persistent launch replayed
-    from a CUDA graph, against the same jobs launched one by one."""
-    import numpy as np
+    binning, orientation count and phase in one CUDA graph (jobs that fill
+    the GPU as their own tuned launches, the rest through one persistent
+    queue kernel), against the same jobs launched one by one and with every
+    job in the queue.  Set-up: one detector set-up per distinct (detector,
+    phase) -- binning does not change the tables -- run concurrently on
+    their own handles, then shared by every job on that detector."""
+    from concurrent.futures import ThreadPoolExecutor
+
     import torch
 
     from ctemsoft_gb300 import capi, synth
@@ -571,30 +644,45 @@ def run_batched(args):
     specs = synth.c3_jobs(2)[:max(1, args.c3_jobs)]
     if args.c3_max_orient > 0:
         specs = [dict(sp, n=min(sp["n"], args.c3_max_orient)) for sp in specs]
-    masters = {}
-    for ph in ("Ni", "Ti"):
-        wl = synth.c3_phase(ph)
-        h = capi.Handle(0)
-        h.set_master(wl.master())
-        masters[ph] = (h, wl.mc())
+    data = {ph: synth.c3_phase(ph) for ph in ("Ni", "Ti")}
+    arrays = {ph: (wl.master(), wl.mc()) for ph, wl in data.items()}
     cache = Path(tempfile.gettempdir()) / "ebsd_autotune.txt"
-    jobs = []
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for sp in specs:
-        mh, acc = masters[sp["phase"]]
+    masters = {}
+    for ph, (sr, acc) in arrays.items():
         h = capi.Handle(0)
-        h.share_master(mh)
-        geom = dict(L=15000.0, thetac=10.0, delta=sp["delta"], numsx=sp["numsx"],
-                    numsy=sp["numsy"], xpc=0.0, ypc=0.0, sig=70.0)
-        num_el = h.set_detector(geom, acc, 1, 11)
-        epi = capi.epilogue(capi.prefactor(15.0, 100.0, num_el), binning=sp["binning"],
+        h.set_master(sr)
+        masters[ph] = h
+    keys = sorted({(sp["numsx"], sp["numsy"], sp["delta"], sp["phase"]) for sp in specs})
+
+    def setup(key):
+        nx, ny, delta, ph = key
+        h = capi.Handle(0)
+        h.share_master(masters[ph])
+        geom = dict(L=15000.0, thetac=10.0, delta=delta, numsx=nx, numsy=ny, xpc=0.0, ypc=0.0,
+                    sig=70.0)
+        h.set_detector(geom, arrays[ph][1], 1, 11)
+        return key, h
+
+    with ThreadPoolExecutor(max_workers=len(keys)) as ex:  # ctypes calls release the GIL
+        dets = dict(ex.map(setup, keys))
+    setup_s = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    jobs = []
+    for sp in specs:
+        src = dets[(sp["numsx"], sp["numsy"], sp["delta"], sp["phase"])]
+        h = capi.Handle(0)
+        h.share_detector(src)
+        epi = capi.epilogue(capi.prefactor(15.0, 100.0, src.num_el), binning=sp["binning"],
                             scalingmode="gam", gammavalue=0.33)
         h.autotune(epi, 64, cache)
         ox, oy = h.output_dims(epi)
         q = torch.from_numpy(synth.shoemake_quaternions(sp["n"], sp["seed"])).to(dev)
         out = torch.empty((sp["n"], oy, ox), device=dev)
         jobs.append((h, q, epi, out))
-    setup_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    tune_s = time.perf_counter() - t1
     total = sum(sp["n"] for sp in specs)
     runner = capi.Handle(0)
     stream = torch.cuda.Stream(dev)
@@ -603,13 +691,18 @@ def run_batched(args):
     for h, *_ in jobs:
         h.set_stream(stream.cuda_stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    # the first batch, end to end after the set-up: graph capture and launch
+    t2 = time.perf_counter()
+    runner.forward_batched(jobs, graph=True)
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t2
 
-    def timed(fn, steps):
+    def timed(fn, n):
         for _ in range(args.warmup):
             fn()
         torch.cuda.synchronize()
         tot = 0.0
-        for _ in range(steps):
+        for _ in range(n):
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -617,44 +710,52 @@ def run_batched(args):
             b.record(stream)
             torch.cuda.synchronize()
             tot += a.elapsed_time(b)
-        return tot / steps
-
-    def batched():
-        runner.forward_batched(jobs, graph=True)
+        return tot / n
 
     queue_runner = capi.Handle(0)
     queue_runner.set_stream(stream.cuda_stream)
-
-    def queued():
-        queue_runner.forward_batched(jobs, graph=True, queue_all=True)
+    ms_b = timed(lambda: runner.forward_batched(jobs, graph=True), steps)
+    ref = [out.clone() for *_, out in jobs]
+    ms_q = timed(lambda: queue_runner.forward_batched(jobs, graph=True, queue_all=True), steps)
+    same_q = all(torch.equal(r, out) for r, (*_, out) in zip(ref, jobs))
 
     def one_by_one():
         for h, q, epi, out in jobs:
             h.forward(q, epi, out=out)
 
-    ms_b = timed(batched, args.steps)
-    ref = [out.clone() for *_, out in jobs]
-    ms_q = timed(queued, args.steps)
-    same_q = all(torch.equal(r, out) for r, (*_, out) in zip(ref, jobs))
-    ms_s = timed(one_by_one, args.steps)
+    ms_s = timed(one_by_one, steps)
     same = all(torch.equal(r, out) for r, (*_, out) in zip(ref, jobs))
-    line = {
+    torch.cuda.set_stream(torch.cuda.default_stream(dev))
+    res = {
         "metric": f"EBSD patterns/s, batched uneven workload ({len(specs)} jobs)",
-        "value": total / (ms_b / 1e3),
-        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_b, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batched-{len(specs)}-jobs-seed2", "patterns": total,
-                   "sizes": sorted({f"{s['numsx']}x{s['numsy']}" for s in specs}),
-                   "launch": "one CUDA graph: jobs that fill the GPU as their own tuned "
-                             "launches, the rest through one persistent queue kernel"},
+        "value": total / (ms_b / 1e3), "unit": UNIT, "ms_per_step": ms_b, "steps": steps,
+        "patterns": total, "detectors": len(keys),
         "one_by_one": {"value": total / (ms_s / 1e3), "ms_per_step": ms_s,
                        "launches": len(jobs)},
         "persistent_only": {"value": total / (ms_q / 1e3), "ms_per_step": ms_q,
                             "identical": bool(same_q),
                             "what": "every job through the persistent queue kernel"},
         "identical_to_one_by_one": bool(same),
-        "setup_s": setup_s,
+        "setup_s": setup_s, "autotune_s": tune_s, "first_batch_s": first_s,
+        "e2e_with_setup": {"value": total / (setup_s + tune_s + first_s), "unit": UNIT,
+                           "what": "detector set-up + launch-shape tuning (cached per shape "
+                                   "in a file) + the first batch (graph capture and run)"},
+        "l2": "flushed (512 MB write) between timed steps",
     }
+    for h, *_ in jobs:
+        h.close()
+    for h in list(dets.values()) + list(masters.values()) + [runner, queue_runner]:
+        h.close()
+    return res
+
+
+def run_batched(args):
+    res = c3_measure(args, args.steps)
+    line = dict(res, n_gpus=1, warmup=args.warmup, higher_is_better=True, dtype="f32",
+                data="synthetic",
+                config={"workload": f"batched-{res['patterns']}-patterns-seed2",
+                        "launch": "one CUDA graph: jobs that fill the GPU as their own tuned "
+                                  "launches, the rest through one persistent queue kernel"})
     print(json.dumps(line))
     return 0
 
@@ -751,7 +852,7 @@ def _apply_steps(q, w):
     return (out / np.linalg.norm(out, axis=1, keepdims=True)).astype(np.float32)
 
 
-def run_gn(args):
+def c5_measure(args, fd_iters: int) -> dict:
     """Gauss-Newton refinement at scale: 100 000 orientations (seed 4) on a
     120x120 detector (480x480 binned 4x4), 15 bins 6-20 keV, targets with
     Poisson noise at 1000 mean counts per detector pixel before binning,
@@ -800,21 +901,27 @@ def run_gn(args):
            "pc_error_px": [geom["xpc"] - true_geom["xpc"], geom["ypc"] - true_geom["ypc"]],
            "L_error_um": geom["L"] - true_geom["L"],
            "config": {"workload": wl.name, "detector": "480x480 binned 4 -> 120x120",
-                      "bins": wl.nEbins, "noise": "Poisson, 1000 counts/px"}}
-    if args.fd_iters > 0:
+                      "bins": wl.nEbins, "energies": "6-20 keV in 1 keV bins",
+                      "noise": "Poisson, 1000 counts/px"}}
+    if fd_iters > 0:
         h.set_detector(g0, acc, 1, wl.nEbins)
         dq = torch.from_numpy(q0).to(dev)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        qf, gf = _fd_gauss_newton(h, dq, clean, targets, g0, acc, args.fd_iters, 1e-3)
+        qf, gf = _fd_gauss_newton(h, dq, clean, targets, g0, acc, fd_iters, 1e-3)
         torch.cuda.synchronize()
         fd_s = time.perf_counter() - t0
         misf = _misorientation_deg(qf.cpu().numpy(), qt)
-        res["forward_only_fd"] = {"iterations": args.fd_iters, "wall_s": fd_s,
-                                  "per_iteration_s": fd_s / args.fd_iters,
+        res["forward_only_fd"] = {"iterations": fd_iters, "wall_s": fd_s,
+                                  "per_iteration_s": fd_s / fd_iters,
                                   "fraction_within_0.01deg": float((misf < 0.01).mean()),
                                   "gn_per_iteration_s": gn_s / max(it, 1)}
-    print(json.dumps(res))
+    h.close()
+    return res
+
+
+def run_gn(args):
+    print(json.dumps(c5_measure(args, args.fd_iters)))
     return 0
 
 

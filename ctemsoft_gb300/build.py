@@ -34,7 +34,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math"
              f"-I{CUDA_HOME / 'include'}"]
 
 CU_SOURCES = ["ebsd_setup.cu", "ebsd_forward.cu", "ebsd_vjp.cu", "ebsd_so3.cu", "ebsd_mc.cu",
-              "ebsd_capi.cu"]
+              "ebsd_membw.cu", "ebsd_capi.cu"]
 CXX_SOURCES = ["ebsd_host.cpp", "ebsd_program.cpp"]
 HEADERS = ["ebsd_internal.h", "ebsd_device.cuh", "ebsd_host.h", "ebsd_noise.cuh"]
 

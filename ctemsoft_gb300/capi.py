@@ -128,6 +128,7 @@ _SIGS = {
     "ebsd_set_option": (C.c_int, [_P, C.c_char_p, C.c_int64]),
     "ebsd_set_master": (C.c_int, [_P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "ebsd_share_master": (C.c_int, [_P, _P]),
+    "ebsd_share_detector": (C.c_int, [_P, _P]),
     "ebsd_set_detector": (C.c_int, [_P, C.POINTER(Geometry), _P, C.c_int32, C.c_int32,
                                     C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     "ebsd_energy_window": (C.c_int, [C.c_float, C.c_float, C.c_double, C.c_double, C.c_int32,
@@ -137,12 +138,18 @@ _SIGS = {
                                    C.POINTER(C.c_int32)]),
     "ebsd_forward": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P]),
     "ebsd_cells": (C.c_int, [_P, _P, C.c_int64, _P, _P, _P, _P]),
+    "ebsd_forward_cells": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P, _P, _P, _P,
+                                     _P]),
     "ebsd_forward_batched": (C.c_int, [_P, C.POINTER(Job), C.c_int32, C.c_int32]),
     "ebsd_gn_accumulate": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P, C.c_double,
                                      _P, _P]),
     "ebsd_gn_apply": (C.c_int, [_P, _P, C.c_int64, C.c_double, _P, C.POINTER(C.c_double)]),
     "ebsd_refine": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), _P, C.POINTER(GNOptions),
                               _P, C.POINTER(Geometry), C.POINTER(C.c_int32)]),
+    "ebsd_refine_sharded": (C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(_P),
+                                      C.POINTER(C.c_int64), C.POINTER(Epilogue), C.POINTER(_P),
+                                      C.POINTER(GNOptions), C.POINTER(_P), C.POINTER(Geometry),
+                                      C.POINTER(C.c_int32)]),
     "ebsd_autotune": (C.c_int, [_P, C.POINTER(Epilogue), C.c_int64, C.c_char_p,
                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                 C.POINTER(C.c_float)]),
@@ -150,6 +157,8 @@ _SIGS = {
     "ebsd_vjp_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(Epilogue), C.c_int32, _P, _P,
                                    _P]),
     "ebsd_get_detector": (C.c_int, [_P, _P, _P, _P, _P]),
+    "ebsd_measure_bandwidth": (C.c_int, [C.c_int32, C.c_int32, C.c_int64, C.c_int32,
+                                         C.POINTER(C.c_double)]),
     "ebsd_sample_rfz": (C.c_int, [_P, C.c_int32, C.c_int32, _P, _P, C.c_int64,
                                   C.POINTER(C.c_int64)]),
     "ebsd_mc_dims": (C.c_int, [C.POINTER(MCParams), C.POINTER(C.c_int32),
@@ -159,6 +168,8 @@ _SIGS = {
     "ebsd_read_mc_namelist": (C.c_int, [C.c_char_p, C.POINTER(MCNamelist)]),
     "ebsd_run_mc_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "ebsd_run_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
+    "ebsd_run_namelist_devices": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.c_int32,
+                                            C.c_int]),
     "ebsd_read_mc_file": (C.c_int, [C.c_char_p, C.POINTER(MCHeader), _P]),
     "ebsd_read_master_file": (C.c_int, [C.c_char_p, C.POINTER(MasterHeader), _P, _P, _P]),
     "ebsd_read_namelist": (C.c_int, [C.c_char_p, C.POINTER(Namelist)]),
@@ -212,6 +223,18 @@ def energy_window(energymin, energymax, Ehistmin, Ebinsize, numEbins):
     _check(lib().ebsd_energy_window(energymin, energymax, Ehistmin, Ebinsize, numEbins,
                                     C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+BW_L1, BW_L2, BW_HBM = 1, 2, 3
+
+
+def measure_bandwidth(device: int, level: int, nbytes: int, repeats: int = 5) -> float:
+    """Read bandwidth (GB/s) of one memory level of a device: BW_L1 (L1 hits,
+    128-bit loads), BW_L2 (an L2-resident working set of nbytes, L1
+    bypassed) or BW_HBM (nbytes larger than L2)."""
+    v = C.c_double()
+    _check(lib().ebsd_measure_bandwidth(device, level, int(nbytes), repeats, C.byref(v)))
+    return v.value
 
 
 def prefactor(beamcurrent, dwelltime, num_el):
@@ -273,6 +296,14 @@ class Handle:
     def share_master(self, other: "Handle"):
         """Use other's master pattern (same device, no copy)."""
         _check(lib().ebsd_share_master(self._h, other._h), self._h)
+
+    def share_detector(self, other: "Handle"):
+        """Use other's master and detector set-up (same device, no copy)."""
+        _check(lib().ebsd_share_detector(self._h, other._h), self._h)
+        self.geometry = dict(other.geometry)
+        self.num_el = other.num_el
+        if hasattr(other, "_nbins"):
+            self._nbins = other._nbins
 
     def set_detector(self, geom: dict, accum_e: np.ndarray, Emin: int, Emax: int) -> int:
         """accum_e: array shaped (2nsy+1, 2nsx+1, numEbins) = Fortran
@@ -389,6 +420,24 @@ class Handle:
                self._h)
         return nix, niy, i0, i1
 
+    def forward_cells(self, quats, epi):
+        """Patterns and Lambert cells from one launch of the pattern kernel
+        (device tensors; returns numpy arrays: out, (nix, niy, ixy0, ixy1))."""
+        import torch
+        q = torch.as_tensor(np.ascontiguousarray(quats, dtype=np.float32)).cuda()
+        n = q.shape[0]
+        ny, nx = self.geometry["numsy"], self.geometry["numsx"]
+        ox, oy = self.output_dims(epi)
+        out = torch.empty((n, oy, ox), dtype=torch.float32, device=q.device)
+        nix = torch.empty((n, ny, nx), dtype=torch.int32, device=q.device)
+        niy = torch.empty_like(nix)
+        i0 = torch.empty((n, ny, nx), dtype=torch.float32, device=q.device)
+        i1 = torch.empty_like(i0)
+        _check(lib().ebsd_forward_cells(self._h, _ptr(q), n, C.byref(epi), _ptr(out), _ptr(nix),
+                                        _ptr(niy), _ptr(i0), _ptr(i1)), self._h)
+        torch.cuda.synchronize()
+        return out.cpu().numpy(), tuple(t.cpu().numpy() for t in (nix, niy, i0, i1))
+
     def get_detector(self, nE: int):
         ny, nx = self.geometry["numsy"], self.geometry["numsx"]
         W = np.empty((ny, nx, nE), np.float32)
@@ -432,8 +481,37 @@ class Handle:
         return r, q
 
 
-def run_namelist(path: str, device: int = 0, quiet: bool = True) -> None:
-    _check(lib().ebsd_run_namelist(str(path).encode(), device, int(quiet)))
+def refine_sharded(handles, quats, epi: Epilogue, targets, max_iterations=20, refine_pc=False,
+                   damping=1e-3, tol_rad=1e-6, tol_pc=1e-4, losses=None):
+    """Gauss-Newton refinement over several handles, each with its shard of
+    device orientations (updated in place) and targets; the pattern-centre
+    system is summed over the shards in this process.  Returns (iterations,
+    refined geometry dict); every handle ends on that geometry."""
+    nh = len(handles)
+    hs = (_P * nh)(*[h.raw.value if hasattr(h.raw, "value") else h.raw for h in handles])
+    qs = (_P * nh)(*[_ptr(q) for q in quats])
+    ts = (_P * nh)(*[_ptr(t) for t in targets])
+    ns = (C.c_int64 * nh)(*[int(q.shape[0]) for q in quats])
+    ls = None if losses is None else (_P * nh)(*[_ptr(x) for x in losses])
+    opt = GNOptions(max_iterations, int(refine_pc), damping, tol_rad, tol_pc)
+    g = Geometry()
+    it = C.c_int32()
+    _check(lib().ebsd_refine_sharded(hs, nh, qs, ns, C.byref(epi), ts, C.byref(opt), ls,
+                                     C.byref(g), C.byref(it)), handles[0].raw)
+    geom = {k: getattr(g, k) for k, _ in Geometry._fields_}
+    for h in handles:
+        h.geometry = dict(geom)
+    return it.value, geom
+
+
+def run_namelist(path: str, device=0, quiet: bool = True) -> None:
+    """The CTEMEBSD program for a namelist file; device is one index or a
+    list of indices (the orientations are split over them)."""
+    if isinstance(device, (list, tuple)):
+        arr = (C.c_int32 * len(device))(*device)
+        _check(lib().ebsd_run_namelist_devices(str(path).encode(), arr, len(device), int(quiet)))
+    else:
+        _check(lib().ebsd_run_namelist(str(path).encode(), device, int(quiet)))
 
 
 def run_mc_namelist(path: str, device: int = 0, quiet: bool = True) -> None:

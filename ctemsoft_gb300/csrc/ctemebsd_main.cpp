@@ -3,11 +3,13 @@
 // Same command line as the reference (files.f90:623-688): an optional
 // namelist file name (default CTEMEBSD.nml), -h for help and -t to write a
 // namelist template into the current folder; any flag stops the program
-// after it is handled.  One addition: -d N selects the CUDA device.
+// after it is handled.  One addition: -d N selects the CUDA device, and
+// -d N,M,... splits the orientations over several devices.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/ebsd_gpu.h"
 
@@ -63,7 +65,8 @@ void usage(const char* prog)
     printf(" If absent, the default name 'CTEMEBSD.nml' will be used.\n");
     printf(" To create a template of the input file, type %s -t\n", prog);
     printf(" To produce this message, type %s -h\n", prog);
-    printf(" -d N runs on CUDA device N (default 0).\n\n");
+    printf(" -d N runs on CUDA device N (default 0); -d N,M,... splits the orientations\n");
+    printf("    over several devices.\n\n");
 }
 
 }  // namespace
@@ -72,7 +75,8 @@ int main(int argc, char** argv)
 {
     std::string nml = "CTEMEBSD.nml";
     bool halt = false;
-    int nonflag = 0, device = 0;
+    int nonflag = 0;
+    std::vector<int32_t> devices;
     for (int i = 1; i < argc; ++i) {
         const char* a = argv[i];
         if (a[0] == '-') {
@@ -90,7 +94,21 @@ int main(int argc, char** argv)
                 printf("  -> created template file CTEMEBSD.template\n");
                 halt = true;
             } else if (!strcmp(a, "-d") && i + 1 < argc) {
-                device = atoi(argv[++i]);
+                devices.clear();
+                for (const char* p = argv[++i]; *p;) {
+                    char* end = nullptr;
+                    const long d = strtol(p, &end, 10);
+                    if (end == p || d < 0 || d > 1024) {
+                        fprintf(stderr, "bad device list %s\n", argv[i]);
+                        return 1;
+                    }
+                    devices.push_back((int32_t)d);
+                    p = *end == ',' ? end + 1 : end;
+                    if (*end && *end != ',') {
+                        fprintf(stderr, "bad device list %s\n", argv[i]);
+                        return 1;
+                    }
+                }
             } else {
                 fprintf(stderr, "unknown option %s\n", a);
                 halt = true;
@@ -105,7 +123,8 @@ int main(int argc, char** argv)
         return 0;
     }
     (void)nonflag;
-    const int rc = ebsd_run_namelist(nml.c_str(), device, 0);
+    if (devices.empty()) devices.push_back(0);
+    const int rc = ebsd_run_namelist_devices(nml.c_str(), devices.data(), (int32_t)devices.size(), 0);
     if (rc != EBSD_OK) {
         fprintf(stderr, "CTEMEBSD: %s (code %d)\n", ebsd_last_error(nullptr), rc);
         return 1;

@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -38,6 +39,43 @@ struct MasterStore {
     }
 };
 
+// Detector tables on one device (direction cosines, weights, derivative
+// tables), shared by every handle that took them with ebsd_share_detector.
+// A handle that changes its geometry while others hold the same tables gets
+// tables of its own first (copy on write), so a sharing handle never sees
+// another's geometry.
+struct DetectorTables {
+    int device = 0;
+    float4* rg = nullptr;
+    float4* W = nullptr;
+    float4* drg = nullptr;
+    float4* dW = nullptr;
+    int P = 0, NV = 0;
+    ~DetectorTables()
+    {
+        cudaSetDevice(device);
+        cudaFree(rg);
+        cudaFree(W);
+        cudaFree(drg);
+        cudaFree(dW);
+        cudaGetLastError();
+    }
+};
+
+// An MC energy histogram uploaded to one device; read-only once uploaded,
+// so handles share it freely.
+struct HistogramStore {
+    int device = 0;
+    int32_t* ptr = nullptr;
+    size_t bytes = 0;
+    ~HistogramStore()
+    {
+        cudaSetDevice(device);
+        cudaFree(ptr);
+        cudaGetLastError();
+    }
+};
+
 struct ebsd_handle {
     int device = 0;
     cudaStream_t own_stream = nullptr;
@@ -59,6 +97,7 @@ struct ebsd_handle {
     ebsd_geometry geom{};
     int Emin = 0, Emax = 0, nsel = 0, NV = 0;
     int32_t num_el = 0;
+    std::shared_ptr<DetectorTables> det;  // owner of the four tables below
     float4* d_rg = nullptr;
     float4* d_W = nullptr;
     float4* d_drg = nullptr;   // [3][P] d rg / d(xpc, ypc, L)
@@ -70,7 +109,7 @@ struct ebsd_handle {
     DeviceBuf quats[2];
     DeviceBuf outb[2];
     DeviceBuf tmp;
-    DeviceBuf accum;           // MC histogram, kept for geometry updates
+    std::shared_ptr<HistogramStore> accum;  // MC histogram, kept for geometry updates
     DeviceBuf small;           // set-up scalars (num_el sum)
     DeviceBuf wref;            // the reference's single-precision weights (num_el)
     DeviceBuf vjp_partial;     // per-CTA partial sums of the adjoint
@@ -94,6 +133,7 @@ struct ebsd_handle {
     int gn_opc = 32;     // Gauss-Newton orientations per CTA
     int weights_fp64 = 1;
     int lambert_accurate = 0;
+    int64_t noise_offset = 0;  // pattern index of a call's first orientation (noise streams)
 
     // batched pattern loop: device job table, pinned host mirror, graph
     DeviceBuf batch_table;
@@ -175,6 +215,27 @@ PtrKind ptr_kind(const void* p)
     }
 }
 
+// Device memory must belong to the handle's GPU: a kernel launched on
+// h->device that dereferences another GPU's memory faults unless peer
+// access happens to be enabled, so such pointers are refused before any
+// launch.  Managed memory (which migrates) and host memory pass.
+int check_device_home(ebsd_handle* h, const char* what, std::initializer_list<const void*> ptrs)
+{
+    for (const void* p : ptrs) {
+        if (!p) continue;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (a.type == cudaMemoryTypeDevice && a.device != h->device)
+            return set_err(h, EBSD_EINVAL,
+                           "%s: pointer %p is memory of device %d; the handle runs on device %d",
+                           what, p, a.device, h->device);
+    }
+    return EBSD_OK;
+}
+
 // Caller device memory that the kernels read or write as float4 (the
 // quaternions) must be 16-byte aligned, doubles 8-byte aligned: a
 // misaligned vector access would fault, so such pointers are refused.
@@ -230,6 +291,7 @@ int fill_params(ebsd_handle* h, const ebsd_epilogue* e, FwdParams& p)
     p.scl = host::lambert_scale(h->npx);
     p.spi2 = host::lambert_spi2_f();
     p.accurate = h->lambert_accurate;
+    p.o_offset = h->noise_offset;
     if (e) {
         if (e->scalingmode < EBSD_SCALING_NOT || e->scalingmode > EBSD_SCALING_GAM)
             return set_err(h, EBSD_EINVAL, "scalingmode %d is not 0 ('not'), 1 ('lin') or 2 ('gam')",
@@ -280,7 +342,7 @@ int check_quats_host(ebsd_handle* h, const float* q, int64_t n)
 int launch_chunk(ebsd_handle* h, FwdParams p, const float4* dq, int64_t n, float* dout,
                  int64_t o_offset = 0, bool host_out = false)
 {
-    p.o_offset = o_offset;
+    p.o_offset += o_offset;
     p.quats = dq;
     p.n = n;
     p.out = dout;
@@ -338,10 +400,9 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
     h->ms.reset();
-    cudaFree(h->d_rg);
-    cudaFree(h->d_W);
-    cudaFree(h->d_drg);
-    cudaFree(h->d_dW);
+    h->det.reset();
+    h->accum.reset();
+    cudaSetDevice(h->device);
     cudaFree(h->vjp_partial.ptr);
     cudaFree(h->vjp_io.ptr);
     for (int i = 0; i < 2; ++i) {
@@ -352,7 +413,6 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
         if (h->ev_d2h[i]) cudaEventDestroy(h->ev_d2h[i]);
     }
     cudaFree(h->tmp.ptr);
-    cudaFree(h->accum.ptr);
     cudaFree(h->small.ptr);
     cudaFree(h->wref.ptr);
     cudaFree(h->gn_sys.ptr);
@@ -421,6 +481,9 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
         if (value < 1 || value > 64)
             return set_err(h, EBSD_EINVAL, "gn_orient_per_cta must be in 1..64");
         h->gn_opc = (int)value;
+    } else if (k == "noise_index_offset") {
+        if (value < 0) return set_err(h, EBSD_EINVAL, "noise_index_offset must be >= 0");
+        h->noise_offset = value;
     } else if (k == "vjp_orient_per_cta") {
         if (value < 1 || value > 64)
             return set_err(h, EBSD_EINVAL, "vjp_orient_per_cta must be in 1..64");
@@ -529,22 +592,27 @@ int detector_setup(ebsd_handle* h, const ebsd_geometry* g, bool with_num_el)
     const int P = g->numsx * g->numsy;
     const int nsel = h->Emax - h->Emin + 1;
     const int NV = (nsel + 3) / 4;
-    if (P != h->P || NV != h->NV || !h->d_rg) {
-        cudaFree(h->d_rg);
-        cudaFree(h->d_W);
-        cudaFree(h->d_drg);
-        cudaFree(h->d_dW);
-        h->d_rg = nullptr;
-        h->d_W = nullptr;
-        h->d_drg = nullptr;
-        h->d_dW = nullptr;
+    // tables of the right size that no other handle holds (copy on write:
+    // a handle sharing them keeps the old ones)
+    if (!h->det || h->det.use_count() > 1 || P != h->det->P || NV != h->det->NV) {
+        h->d_rg = h->d_W = h->d_drg = h->d_dW = nullptr;
         h->P = 0;
-        CK(h, cudaMalloc(&h->d_rg, sizeof(float4) * (size_t)P), "cudaMalloc rg");
-        CK(h, cudaMalloc(&h->d_W, sizeof(float4) * (size_t)P * NV), "cudaMalloc W");
-        CK(h, cudaMalloc(&h->d_drg, sizeof(float4) * (size_t)P * 3), "cudaMalloc drg");
-        CK(h, cudaMalloc(&h->d_dW, sizeof(float4) * (size_t)P * (2 * NV + 1)), "cudaMalloc dW");
+        h->det.reset();
+        auto t = std::make_shared<DetectorTables>();
+        t->device = h->device;
+        CK(h, cudaMalloc(&t->rg, sizeof(float4) * (size_t)P), "cudaMalloc rg");
+        CK(h, cudaMalloc(&t->W, sizeof(float4) * (size_t)P * NV), "cudaMalloc W");
+        CK(h, cudaMalloc(&t->drg, sizeof(float4) * (size_t)P * 3), "cudaMalloc drg");
+        CK(h, cudaMalloc(&t->dW, sizeof(float4) * (size_t)P * (2 * NV + 1)), "cudaMalloc dW");
+        t->P = P;
+        t->NV = NV;
+        h->det = std::move(t);
     }
-    const int32_t* acc = (const int32_t*)h->accum.ptr;
+    h->d_rg = h->det->rg;
+    h->d_W = h->det->W;
+    h->d_drg = h->det->drg;
+    h->d_dW = h->det->dW;
+    const int32_t* acc = h->accum->ptr;
     float ca, sa;
     host::detector_angles(g->sig, g->thetac, &ca, &sa);
     CK(h, launch_detector(*g, ca, sa, h->d_rg, s), "detector kernel");
@@ -629,13 +697,20 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
         h->il_bytes = it->second.second;
     }
 
-    // the histogram stays on the device for later geometry updates
+    // the histogram stays on the device for later geometry updates (in a
+    // store of this handle's own: a shared one is left to its other holders)
     const size_t acc_bytes = sizeof(int32_t) * (size_t)numEbins * (2 * nsx + 1) * (2 * nsy + 1);
-    rc = ensure(h, h->accum, acc_bytes, "MC histogram");
-    if (rc) return rc;
+    if (!h->accum || h->accum.use_count() > 1 || h->accum->bytes != acc_bytes) {
+        h->accum.reset();
+        auto a = std::make_shared<HistogramStore>();
+        a->device = h->device;
+        CK(h, cudaMalloc(&a->ptr, acc_bytes), "cudaMalloc MC histogram");
+        a->bytes = acc_bytes;
+        h->accum = std::move(a);
+    }
     rc = ensure(h, h->small, 256, "set-up scalars");
     if (rc) return rc;
-    CK(h, cudaMemcpyAsync(h->accum.ptr, accum_e, acc_bytes, cudaMemcpyHostToDevice, s),
+    CK(h, cudaMemcpyAsync(h->accum->ptr, accum_e, acc_bytes, cudaMemcpyHostToDevice, s),
        "MC upload");
     h->Emin = Emin;
     h->Emax = Emax;
@@ -664,6 +739,52 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
     return EBSD_OK;
 }
 
+extern "C" int ebsd_share_detector(ebsd_handle* dst, const ebsd_handle* src)
+{
+    if (!dst || !src) return set_err(dst, EBSD_EINVAL, "ebsd_share_detector: null handle");
+    if (dst == src) return EBSD_OK;
+    if (!src->have_master || !src->have_detector)
+        return set_err(dst, EBSD_ESTATE, "ebsd_share_detector: the source handle has no detector");
+    if (src->device != dst->device)
+        return set_err(dst, EBSD_EINVAL, "ebsd_share_detector: handles are on devices %d and %d",
+                       src->device, dst->device);
+    int rc = activate(dst);
+    if (rc) return rc;
+    // nothing of dst's may still be running on the tables it gives up
+    CK(dst, cudaStreamSynchronize(dst->stream), "ebsd_share_detector");
+    rc = ensure(dst, dst->small, 256, "set-up scalars");
+    if (rc) return rc;
+    dst->ms = src->ms;
+    dst->npx = src->npx;
+    dst->npy = src->npy;
+    dst->nE = src->nE;
+    dst->numset = src->numset;
+    dst->have_master = true;
+    dst->d_master_il = src->d_master_il;
+    dst->il_bytes = src->il_bytes;
+    dst->det = src->det;
+    dst->d_rg = src->d_rg;
+    dst->d_W = src->d_W;
+    dst->d_drg = src->d_drg;
+    dst->d_dW = src->d_dW;
+    dst->accum = src->accum;
+    dst->geom = src->geom;
+    dst->Emin = src->Emin;
+    dst->Emax = src->Emax;
+    dst->nsel = src->nsel;
+    dst->NV = src->NV;
+    dst->num_el = src->num_el;
+    dst->P = src->P;
+    dst->nsx = src->nsx;
+    dst->nsy = src->nsy;
+    dst->weights_fp64 = src->weights_fp64;
+    dst->cfg.persist_base = src->cfg.persist_base;
+    dst->cfg.persist_bytes = src->cfg.persist_bytes;
+    dst->cfg.persist_hit_ratio = src->cfg.persist_hit_ratio;
+    dst->have_detector = true;
+    return EBSD_OK;
+}
+
 extern "C" int ebsd_output_dims(const ebsd_handle* hc, const ebsd_epilogue* e, int32_t* nx,
                                 int32_t* ny)
 {
@@ -686,6 +807,8 @@ extern "C" int ebsd_forward(ebsd_handle* h, const float* quats, int64_t n, const
     if (n < 0) return set_err(h, EBSD_EINVAL, "negative orientation count");
     if (n == 0) return EBSD_OK;
     if (!quats || !out || !e) return set_err(h, EBSD_EINVAL, "ebsd_forward: null argument");
+    rc = check_device_home(h, "ebsd_forward", {quats, out});
+    if (rc) return rc;
     rc = activate(h);
     if (rc) return rc;
     FwdParams p;
@@ -827,6 +950,8 @@ extern "C" int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebs
     if (n < 0) return set_err(h, EBSD_EINVAL, "negative orientation count");
     if (n == 0) return EBSD_OK;
     if (!quats || !e || !data || !grad) return set_err(h, EBSD_EINVAL, "ebsd_vjp: null argument");
+    rc = check_device_home(h, "ebsd_vjp", {quats, data, loss, grad});
+    if (rc) return rc;
     if (mode != EBSD_VJP_COTANGENT && mode != EBSD_VJP_NDP)
         return set_err(h, EBSD_EINVAL, "ebsd_vjp: unknown mode %d", mode);
     if (e->scalingmode == EBSD_SCALING_GAM || e->poisson)
@@ -941,7 +1066,11 @@ std::mutex g_scratch_mu;
 float* g_scratch_addr[kMaxDevicesNoAlloc] = {};
 
 // Device address of g_vjp_scratch on the current device (host code may
-// only use the symbol through this address).  Looked up once per device.
+// only use the symbol through this address).  Looked up once per device, on
+// the first call on that device, and kept for the life of the process: a
+// cudaDeviceReset, which also destroys every handle's device state, leaves
+// the cached address stale, so this entry point must not be used after a
+// reset of its device.
 int scratch_address(ebsd_handle* h, float** out)
 {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
@@ -984,6 +1113,8 @@ extern "C" int ebsd_vjp_noalloc(ebsd_handle* h, const float* quats, int64_t n,
         (loss && ptr_kind(loss) != kDevice))
         return set_err(h, EBSD_EINVAL,
                        "ebsd_vjp_noalloc: quats, data, loss and grad must be device memory");
+    rc = check_device_home(h, "ebsd_vjp_noalloc", {quats, data, loss, grad});
+    if (rc) return rc;
     rc = check_aligned(h, quats, 16, "ebsd_vjp_noalloc quats");
     if (rc) return rc;
     rc = activate(h);
@@ -1043,6 +1174,8 @@ int gn_check(ebsd_handle* h, const ebsd_epilogue* e, const float* quats, const f
     if (h->NV > 8) return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: at most 32 energy bins");
     if (ptr_kind(quats) != kDevice || ptr_kind(targets) != kDevice)
         return set_err(h, EBSD_EINVAL, "Gauss-Newton: quats and targets must be device memory");
+    const int rc = check_device_home(h, "Gauss-Newton", {quats, targets});
+    if (rc) return rc;
     return check_aligned(h, quats, 16, "Gauss-Newton quats");
 }
 
@@ -1059,6 +1192,8 @@ extern "C" int ebsd_gn_accumulate(ebsd_handle* h, const float* quats, int64_t n,
     if (rc) return rc;
     if (loss && ptr_kind(loss) != kDevice)
         return set_err(h, EBSD_EINVAL, "ebsd_gn_accumulate: loss must be device memory");
+    rc = check_device_home(h, "ebsd_gn_accumulate", {loss});
+    if (rc) return rc;
     rc = activate(h);
     if (rc) return rc;
     FwdParams p;
@@ -1121,6 +1256,8 @@ extern "C" int ebsd_gn_apply(ebsd_handle* h, float* quats, int64_t n, double dam
                        "had %lld", (long long)n, (long long)h->gn_n);
     if (!quats || ptr_kind(quats) != kDevice)
         return set_err(h, EBSD_EINVAL, "ebsd_gn_apply: quats must be device memory");
+    rc = check_device_home(h, "ebsd_gn_apply", {quats});
+    if (rc) return rc;
     rc = check_aligned(h, quats, 16, "ebsd_gn_apply quats");
     if (rc) return rc;
     rc = activate(h);
@@ -1210,6 +1347,105 @@ extern "C" int ebsd_refine(ebsd_handle* h, float* quats, int64_t n, const ebsd_e
     return EBSD_OK;
 }
 
+extern "C" int ebsd_refine_sharded(ebsd_handle* const* hs, int32_t nh, float* const* quats,
+                                   const int64_t* n, const ebsd_epilogue* e,
+                                   const float* const* targets, const ebsd_gn_options* opt,
+                                   float* const* loss, ebsd_geometry* geom, int32_t* iterations)
+{
+    if (!hs || nh < 1 || nh > 64 || !quats || !n || !targets)
+        return set_err(nullptr, EBSD_EINVAL, "ebsd_refine_sharded: bad handle or shard lists");
+    ebsd_handle* h0 = hs[0];
+    for (int k = 0; k < nh; ++k) {
+        int rc = check_ready(hs[k]);
+        if (rc) return rc;
+        if (hs[k]->geom.numsx != h0->geom.numsx || hs[k]->geom.numsy != h0->geom.numsy ||
+            memcmp(&hs[k]->geom, &h0->geom, sizeof(ebsd_geometry)) != 0)
+            return set_err(h0, EBSD_EINVAL, "ebsd_refine_sharded: handle %d has another detector "
+                           "geometry than handle 0", k);
+        for (int j = 0; j < k; ++j)
+            if (hs[j] == hs[k])
+                return set_err(h0, EBSD_EINVAL, "ebsd_refine_sharded: handle %d listed twice", k);
+    }
+    if (!opt || opt->max_iterations < 0)
+        return set_err(h0, EBSD_EINVAL, "ebsd_refine_sharded: options");
+    if (opt->refine_pc && !geom)
+        return set_err(h0, EBSD_EINVAL, "ebsd_refine_sharded: refine_pc needs the geometry");
+    // run f(k) for every shard with orientations, each on its own host thread;
+    // the first failing shard's message goes to handle 0
+    std::vector<int> rcs(nh, EBSD_OK);
+    auto each = [&](auto f) -> int {
+        std::vector<std::thread> th;
+        for (int k = 0; k < nh; ++k)
+            if (n[k] > 0) th.emplace_back([&, k] { rcs[k] = f(k); });
+        for (auto& t : th) t.join();
+        for (int k = 0; k < nh; ++k)
+            if (rcs[k]) {
+                if (k) set_err(h0, rcs[k], "shard %d: %s", k, std::string(hs[k]->err).c_str());
+                return rcs[k];
+            }
+        return EBSD_OK;
+    };
+    std::vector<double> sys((size_t)nh * 12), steps(nh);
+    ebsd_geometry g = h0->geom;
+    int it = 0, rc = EBSD_OK;
+    for (; it < opt->max_iterations; ++it) {
+        rc = each([&](int k) {
+            return ebsd_gn_accumulate(hs[k], quats[k], n[k], e, targets[k], opt->damping,
+                                      opt->refine_pc ? &sys[12 * k] : nullptr,
+                                      loss ? loss[k] : nullptr);
+        });
+        if (rc) return rc;
+        // the pattern-centre system: the sum over shards, in shard order
+        double sum[12] = {0.0};
+        for (int k = 0; k < nh; ++k)
+            if (n[k] > 0)
+                for (int i = 0; i < 12; ++i) sum[i] += sys[12 * k + i];
+        double dpc[3] = {0.0, 0.0, 0.0};
+        if (opt->refine_pc && !solve3(sum, sum + 9, opt->damping, dpc))
+            dpc[0] = dpc[1] = dpc[2] = 0.0;
+        rc = each([&](int k) {
+            return ebsd_gn_apply(hs[k], quats[k], n[k], opt->damping,
+                                 opt->refine_pc ? dpc : nullptr, &steps[k]);
+        });
+        if (rc) return rc;
+        double mstep = 0.0;
+        for (int k = 0; k < nh; ++k)
+            if (n[k] > 0) mstep = std::max(mstep, steps[k]);
+        const double pcstep = std::max(std::fabs(dpc[0]), std::max(std::fabs(dpc[1]),
+                                                                   std::fabs(dpc[2])));
+        if (opt->refine_pc && pcstep > 0.0) {
+            g.xpc = (float)((double)g.xpc + dpc[0]);
+            g.ypc = (float)((double)g.ypc + dpc[1]);
+            g.L = (float)((double)g.L + dpc[2]);
+            for (int k = 0; k < nh; ++k) {  // every handle, including idle shards
+                rc = activate(hs[k]);
+                if (!rc) rc = detector_setup(hs[k], &g, false);
+                if (rc) {
+                    if (k) set_err(h0, rc, "shard %d: %s", k, std::string(hs[k]->err).c_str());
+                    return rc;
+                }
+            }
+        }
+        if (mstep < opt->tol_rad && (!opt->refine_pc || pcstep < opt->tol_pc)) {
+            ++it;
+            break;
+        }
+    }
+    if (loss) {  // loss at the final estimate
+        rc = each([&](int k) {
+            int r = ebsd_gn_accumulate(hs[k], quats[k], n[k], e, targets[k], opt->damping,
+                                       nullptr, loss[k]);
+            if (!r && cudaStreamSynchronize(hs[k]->stream) != cudaSuccess)
+                r = cuda_err(hs[k], cudaGetLastError(), "refine");
+            return r;
+        });
+        if (rc) return rc;
+    }
+    if (geom) *geom = h0->geom;
+    if (iterations) *iterations = it;
+    return EBSD_OK;
+}
+
 // ----------------------------------------------------------------------
 // Batched pattern loop
 
@@ -1261,6 +1497,8 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         if (!J.quats || !J.out) return set_err(h, EBSD_EINVAL, "job %d: null pointer", j);
         if (ptr_kind(J.quats) != kDevice || ptr_kind(J.out) != kDevice)
             return set_err(h, EBSD_EINVAL, "job %d: quats and out must be device memory", j);
+        if (check_device_home(h, "ebsd_forward_batched", {J.quats, J.out}))
+            return set_err(h, EBSD_EINVAL, "job %d: %s", j, std::string(h->err).c_str());
         if (((uintptr_t)J.quats & 15) != 0)
             return set_err(h, EBSD_EINVAL, "job %d: quats not 16-byte aligned", j);
         if (src->NV > 8)
@@ -1570,6 +1808,54 @@ extern "C" int ebsd_autotune(ebsd_handle* h, const ebsd_epilogue* e, int64_t n_s
     return EBSD_OK;
 }
 
+namespace {
+
+// One launch of the pattern kernel's diagnostic instantiation: patterns
+// into dout and the Lambert cells of every (orientation, pixel) into the
+// four device arrays, all on the handle's stream.
+int forward_cells_device(ebsd_handle* h, FwdParams p, const float4* dq, int64_t n, float* dout,
+                         int32_t* nix, int32_t* niy, float* ixy0, float* ixy1)
+{
+    p.quats = dq;
+    p.n = n;
+    p.out = dout;
+    p.nix = nix;
+    p.niy = niy;
+    p.ixy0 = ixy0;
+    p.ixy1 = ixy1;
+    cudaError_t e = launch_forward(p, h->NV, h->cfg, h->stream, true);
+    if (e != cudaSuccess) return cuda_err(h, e, "pattern kernel (cells) launch");
+    return EBSD_OK;
+}
+
+}  // namespace
+
+extern "C" int ebsd_forward_cells(ebsd_handle* h, const float* quats, int64_t n,
+                                  const ebsd_epilogue* e, float* out, int32_t* nix, int32_t* niy,
+                                  float* ixy0, float* ixy1)
+{
+    int rc = check_ready(h);
+    if (rc) return rc;
+    if (n < 0 || !quats || !e || !out || !nix || !niy || !ixy0 || !ixy1)
+        return set_err(h, EBSD_EINVAL, "ebsd_forward_cells: invalid arguments");
+    if (n == 0) return EBSD_OK;
+    if (e->poisson)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_forward_cells: no noise in the cells variant");
+    if (ptr_kind(quats) != kDevice || ptr_kind(out) != kDevice || ptr_kind(nix) != kDevice ||
+        ptr_kind(niy) != kDevice || ptr_kind(ixy0) != kDevice || ptr_kind(ixy1) != kDevice)
+        return set_err(h, EBSD_EINVAL, "ebsd_forward_cells: every array must be device memory");
+    rc = check_device_home(h, "ebsd_forward_cells", {quats, out, nix, niy, ixy0, ixy1});
+    if (rc) return rc;
+    rc = check_aligned(h, quats, 16, "ebsd_forward_cells quats");
+    if (rc) return rc;
+    rc = activate(h);
+    if (rc) return rc;
+    FwdParams p;
+    rc = fill_params(h, e, p);
+    if (rc) return rc;
+    return forward_cells_device(h, p, (const float4*)quats, n, out, nix, niy, ixy0, ixy1);
+}
+
 extern "C" int ebsd_cells(ebsd_handle* h, const float* quats, int64_t n, int32_t* nix,
                           int32_t* niy, float* ixy0, float* ixy1)
 {
@@ -1578,54 +1864,69 @@ extern "C" int ebsd_cells(ebsd_handle* h, const float* quats, int64_t n, int32_t
     if (n < 0 || !quats || !nix || !niy || !ixy0 || !ixy1)
         return set_err(h, EBSD_EINVAL, "ebsd_cells: invalid arguments");
     if (n == 0) return EBSD_OK;
+    rc = check_device_home(h, "ebsd_cells", {quats, nix, niy, ixy0, ixy1});
+    if (rc) return rc;
     rc = activate(h);
     if (rc) return rc;
+    ebsd_epilogue unit;
+    memset(&unit, 0, sizeof unit);
+    unit.prefactor = 1.0;
+    unit.binning = 1;
+    unit.scalingmode = EBSD_SCALING_NOT;
     FwdParams p;
-    rc = fill_params(h, nullptr, p);
+    rc = fill_params(h, &unit, p);
     if (rc) return rc;
     const size_t total = (size_t)n * h->P;
-    const bool dev = ptr_kind(nix) == kDevice;
+    const bool dev = ptr_kind(nix) == kDevice && ptr_kind(niy) == kDevice &&
+                     ptr_kind(ixy0) == kDevice && ptr_kind(ixy1) == kDevice;
     cudaStream_t s = h->stream;
+    // call-local buffers: quaternions (host input), the patterns the
+    // kernel also writes, and the cells when the caller's are on the host
     DeviceBuf qb, ob;
     const float4* dq = (const float4*)quats;
-    if (ptr_kind(quats) == kDevice) {
+    const bool qdev = ptr_kind(quats) == kDevice;
+    if (qdev) {
         rc = check_aligned(h, quats, 16, "ebsd_cells quats");
         if (rc) return rc;
     } else {
-        rc = ensure(h, qb, sizeof(float4) * n, "quaternions");
+        rc = check_quats_host(h, quats, n);
         if (rc) return rc;
-        CK(h, cudaMemcpyAsync(qb.ptr, quats, sizeof(float4) * n, cudaMemcpyHostToDevice, s), "upload");
-        dq = (const float4*)qb.ptr;
     }
-    p.quats = dq;
-    p.n = n;
-    if (dev) {
-        p.nix = nix;
-        p.niy = niy;
-        p.ixy0 = ixy0;
-        p.ixy1 = ixy1;
-    } else {
-        rc = ensure(h, ob, total * 16, "cells");
-        if (rc) {
-            cudaFree(qb.ptr);
-            return rc;
+    const size_t qbytes = qdev ? 0 : ((sizeof(float4) * n + 255) & ~size_t(255));
+    const size_t pbytes = (total * 4 + 255) & ~size_t(255);
+    rc = ensure(h, ob, qbytes + pbytes + (dev ? 0 : total * 16), "cells staging");
+    if (rc) return rc;
+    char* base = (char*)ob.ptr;
+    if (!qdev) {
+        dq = (const float4*)base;
+        cudaError_t ce =
+            cudaMemcpyAsync(base, quats, sizeof(float4) * n, cudaMemcpyHostToDevice, s);
+        if (ce != cudaSuccess) {
+            cudaFree(ob.ptr);
+            return cuda_err(h, ce, "ebsd_cells upload");
         }
-        char* base = (char*)ob.ptr;
-        p.nix = (int32_t*)base;
-        p.niy = (int32_t*)(base + total * 4);
-        p.ixy0 = (float*)(base + total * 8);
-        p.ixy1 = (float*)(base + total * 12);
     }
-    cudaError_t e = launch_cells(p, h->NV, s);
-    if (e == cudaSuccess && !dev) {
-        e = cudaMemcpyAsync(nix, p.nix, total * 4, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(niy, p.niy, total * 4, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(ixy0, p.ixy0, total * 4, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(ixy1, p.ixy1, total * 4, cudaMemcpyDeviceToHost, s);
+    float* dpat = (float*)(base + qbytes);
+    int32_t *dnix = nix, *dniy = niy;
+    float *d0 = ixy0, *d1 = ixy1;
+    if (!dev) {
+        char* c = base + qbytes + pbytes;
+        dnix = (int32_t*)c;
+        dniy = (int32_t*)(c + total * 4);
+        d0 = (float*)(c + total * 8);
+        d1 = (float*)(c + total * 12);
+    }
+    rc = forward_cells_device(h, p, dq, n, dpat, dnix, dniy, d0, d1);
+    cudaError_t e = cudaSuccess;
+    if (!rc && !dev) {
+        e = cudaMemcpyAsync(nix, dnix, total * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(niy, dniy, total * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ixy0, d0, total * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ixy1, d1, total * 4, cudaMemcpyDeviceToHost, s);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    cudaFree(qb.ptr);
     cudaFree(ob.ptr);
+    if (rc) return rc;
     if (e != cudaSuccess) return cuda_err(h, e, "ebsd_cells");
     return EBSD_OK;
 }
@@ -1723,6 +2024,8 @@ extern "C" int ebsd_sample_rfz(ebsd_handle* h, int32_t nsteps, int32_t pgnum, do
     const bool want = capacity > 0 && (rods || quats);
     const bool rdev = rods && ptr_kind(rods) == kDevice;
     const bool qdev = quats && ptr_kind(quats) == kDevice;
+    rc = check_device_home(h, "ebsd_sample_rfz", {rods, quats});
+    if (rc) return rc;
     if (rdev) {
         rc = check_aligned(h, rods, 8, "ebsd_sample_rfz rods");
         if (rc) return rc;
@@ -1804,6 +2107,8 @@ extern "C" int ebsd_mc_run(ebsd_handle* h, const ebsd_mc_params* p, uint64_t see
     const size_t nzs = (size_t)nE * nz * w10 * w10;
     const bool edev = ptr_kind(accum_e) == kDevice;
     const bool zdev = accum_z ? ptr_kind(accum_z) == kDevice : true;
+    rc = check_device_home(h, "ebsd_mc_run", {accum_e, accum_z});
+    if (rc) return rc;
     const size_t o_cnt = 0, o_e = 256;
     const size_t o_z = o_e + (edev ? 0 : ((ne * 4 + 255) & ~size_t(255)));
     rc = ensure(h, h->mc, o_z + (zdev ? 0 : nzs * 4) + 256, "Monte-Carlo histograms");
@@ -1825,5 +2130,30 @@ extern "C" int ebsd_mc_run(ebsd_handle* h, const ebsd_mc_params* p, uint64_t see
         CK(h, cudaMemcpyAsync(accum_z, dz, nzs * 4, cudaMemcpyDeviceToHost, s), "accum_z copy");
     CK(h, cudaStreamSynchronize(s), "Monte-Carlo");
     if (counted) *counted = (int64_t)c;
+    return EBSD_OK;
+}
+
+// ----------------------------------------------------------------------
+// Roofline denominators
+
+extern "C" int ebsd_measure_bandwidth(int32_t device, int32_t level, int64_t bytes,
+                                      int32_t repeats, double* gbs)
+{
+    if (!gbs) return set_err(nullptr, EBSD_EINVAL, "ebsd_measure_bandwidth: null output");
+    if (level != EBSD_BW_L1 && level != EBSD_BW_L2 && level != EBSD_BW_HBM)
+        return set_err(nullptr, EBSD_EINVAL, "ebsd_measure_bandwidth: unknown level %d", level);
+    if (bytes < 16 || bytes > (int64_t(64) << 30) || repeats < 1 || repeats > 1000)
+        return set_err(nullptr, EBSD_EINVAL,
+                       "ebsd_measure_bandwidth: bytes in 16 B..64 GiB, repeats in 1..1000");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return set_err(nullptr, EBSD_EINVAL, "ebsd_measure_bandwidth: no device %d", device);
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaError_t e = measure_read_bandwidth(device, level, bytes, repeats, gbs, nullptr);
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_err(nullptr, e, "ebsd_measure_bandwidth");
     return EBSD_OK;
 }

@@ -128,8 +128,12 @@ __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, fl
 // [o_begin, o_begin + opc).  `tile` is shared scratch of tile_y x 33 floats.
 // BIN8: the variant for 8x8-binned records outside the reference-order mode
 // (its pair barriers are kept out of the other variants, where their
-// reservation would cost occupancy).
-template <int NV, bool STRICT, bool NOISE, bool BIN8 = false>
+// reservation would cost occupancy).  CELLS: the same kernel also stores
+// each pixel's Lambert cell and coordinates (prm.nix, niy, ixy0, ixy1, one
+// value per orientation and detector pixel) -- a diagnostic instantiation
+// of this template, so that cell parity is read out of the code that makes
+// the patterns.
+template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false>
 __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, int tiles_x, int t,
                                              int64_t o_begin, int opc, float* tile, int bw)
 {
@@ -187,6 +191,13 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
             const int ix0 = lambert_cell(ixy0, prm.npx, dx, nix);
             const int iy0 = lambert_cell(ixy1, prm.npy, dy, niy);
             const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
+            if (CELLS) {
+                const int64_t ci = o * (int64_t)prm.P + p;
+                prm.nix[ci] = nix;
+                prm.niy[ci] = niy;
+                prm.ixy0[ci] = ixy0;
+                prm.ixy1[ci] = ixy1;
+            }
             const float acc =
                 gather_pixel<NV, STRICT>(prm.master, prm.gx, ix0, iy0, ix1, iy1, dx, dy, w, pol);
             // :608 -- binary64 in the reference order; otherwise one binary32
@@ -292,14 +303,15 @@ int resolve_opc(int opc, int64_t n, int ntiles)
 #define EBSD_FWD_LAUNCH_BOUNDS __launch_bounds__(512)
 #endif
 
-template <int NV, bool STRICT, bool NOISE, bool BIN8>
+template <int NV, bool STRICT, bool NOISE, bool BIN8, bool CELLS = false>
 __global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y, int tiles_x,
                                                  int ntiles, int opc, int warp_w)
 {
     extern __shared__ float tile[];  // [tile_y][33], binning only
     const int t = (int)(blockIdx.x % (unsigned)ntiles);
     const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
-    forward_tile<NV, STRICT, NOISE, BIN8>(prm, tile_y, tiles_x, t, o_begin, opc, tile, warp_w);
+    forward_tile<NV, STRICT, NOISE, BIN8, CELLS>(prm, tile_y, tiles_x, t, o_begin, opc, tile,
+                                                 warp_w);
 }
 
 // Batched pattern loop: one persistent grid works through a queue of work
@@ -378,27 +390,7 @@ __global__ void __launch_bounds__(32 * TY, TY == 4 ? EBSD_BATCH_MIN_BLOCKS4 : 32
     }
 }
 
-// Cell diagnostics: nix/niy/ixy per pixel and orientation.
-__global__ void k_cells(const FwdParams prm)
-{
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t total = prm.n * prm.P;
-    if (idx >= total) return;
-    const int64_t o = idx / prm.P;
-    const int p = (int)(idx - o * prm.P);
-    float ixy0, ixy1;
-    pixel_lambert(prm.quats[o], prm.rg[p], prm.scl, prm.spi2, prm.accurate != 0, ixy0, ixy1);
-    float dx, dy;
-    int nix, niy;
-    lambert_cell(ixy0, prm.npx, dx, nix);
-    lambert_cell(ixy1, prm.npy, dy, niy);
-    prm.nix[idx] = nix;
-    prm.niy[idx] = niy;
-    prm.ixy0[idx] = ixy0;
-    prm.ixy1[idx] = ixy1;
-}
-
-template <int NV, bool STRICT, bool NOISE, bool BIN8 = false>
+template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false>
 cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
     // binned records are summed inside a CTA: its height must hold whole
@@ -421,14 +413,18 @@ cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
     cudaLaunchAttribute attr[1];
     set_persist_attr(cfg, attr, lc);
     const int warp_w = cfg.warp_w == 32 ? 32 : 16;
-    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE, BIN8>, p, tile_y, tiles_x, ntiles, opc,
-                              warp_w);
+    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE, BIN8, CELLS>, p, tile_y, tiles_x,
+                              ntiles, opc, warp_w);
 }
 
 template <int NV>
-cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
+cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s, bool cells)
 {
     const bool bin8 = !cfg.strict && p.mode != EBSD_SCALING_NOT && p.binning == 8;
+    if (cells)  // the diagnostic instantiations (no noise)
+        return cfg.strict ? launch_nv2<NV, true, false, false, true>(p, cfg, s)
+               : bin8     ? launch_nv2<NV, false, false, true, true>(p, cfg, s)
+                          : launch_nv2<NV, false, false, false, true>(p, cfg, s);
     if (p.poisson)  // noise: fused gather
         return bin8 ? launch_nv2<NV, false, true, true>(p, cfg, s)
                     : launch_nv2<NV, false, true>(p, cfg, s);
@@ -520,39 +516,30 @@ int64_t forward_ctas(const FwdParams& p, const LaunchCfg& cfg)
     return ((p.n + opc - 1) / opc) * (int64_t)ntiles;
 }
 
-cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s)
+cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s,
+                           bool cells)
 {
     if (p.n <= 0) return cudaSuccess;
+    if (cells && (!p.nix || !p.niy || !p.ixy0 || !p.ixy1)) return cudaErrorInvalidValue;
     switch (NV) {
-        case 1: return launch_nv<1>(p, cfg, s);
-        case 2: return launch_nv<2>(p, cfg, s);
-        case 3: return launch_nv<3>(p, cfg, s);
-        case 4: return launch_nv<4>(p, cfg, s);
-        case 5: return launch_nv<5>(p, cfg, s);
-        case 6: return launch_nv<6>(p, cfg, s);
-        case 7: return launch_nv<7>(p, cfg, s);
-        case 8: return launch_nv<8>(p, cfg, s);
-        case 9: return launch_nv<9>(p, cfg, s);
-        case 10: return launch_nv<10>(p, cfg, s);
-        case 11: return launch_nv<11>(p, cfg, s);
-        case 12: return launch_nv<12>(p, cfg, s);
-        case 13: return launch_nv<13>(p, cfg, s);
-        case 14: return launch_nv<14>(p, cfg, s);
-        case 15: return launch_nv<15>(p, cfg, s);
-        case 16: return launch_nv<16>(p, cfg, s);
+        case 1: return launch_nv<1>(p, cfg, s, cells);
+        case 2: return launch_nv<2>(p, cfg, s, cells);
+        case 3: return launch_nv<3>(p, cfg, s, cells);
+        case 4: return launch_nv<4>(p, cfg, s, cells);
+        case 5: return launch_nv<5>(p, cfg, s, cells);
+        case 6: return launch_nv<6>(p, cfg, s, cells);
+        case 7: return launch_nv<7>(p, cfg, s, cells);
+        case 8: return launch_nv<8>(p, cfg, s, cells);
+        case 9: return launch_nv<9>(p, cfg, s, cells);
+        case 10: return launch_nv<10>(p, cfg, s, cells);
+        case 11: return launch_nv<11>(p, cfg, s, cells);
+        case 12: return launch_nv<12>(p, cfg, s, cells);
+        case 13: return launch_nv<13>(p, cfg, s, cells);
+        case 14: return launch_nv<14>(p, cfg, s, cells);
+        case 15: return launch_nv<15>(p, cfg, s, cells);
+        case 16: return launch_nv<16>(p, cfg, s, cells);
         default: return cudaErrorInvalidValue;
     }
-}
-
-cudaError_t launch_cells(const FwdParams& p, int /*NV*/, cudaStream_t s)
-{
-    const int64_t total = p.n * p.P;
-    if (total <= 0) return cudaSuccess;
-    const int bs = 256;
-    const int64_t blocks = (total + bs - 1) / bs;
-    if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    k_cells<<<(unsigned)blocks, bs, 0, s>>>(p);
-    return cudaGetLastError();
 }
 
 }  // namespace ebsd

@@ -41,7 +41,7 @@ struct FwdParams {
     uint64_t seed;
     int64_t o_offset;      // index of quats[0] within the call (noise streams)
     int accurate;          // cancellation-free 1 - z near the poles
-    // diagnostics (cells mode)
+    // diagnostics (the cells instantiation of the pattern kernel): [n][P]
     int32_t* nix;
     int32_t* niy;
     float* ixy0;
@@ -138,11 +138,16 @@ cudaError_t launch_gn_schur(const double* sys, int64_t n, double lambda, double*
 cudaError_t launch_gn_update(const double* sys, int64_t n, double lambda, const double* dpc,
                              float4* quats, float* step, cudaStream_t s);
 
+// Memory-hierarchy read bandwidth (ebsd_membw.cu), level EBSD_BW_*.
+cudaError_t measure_read_bandwidth(int device, int level, long long bytes, int repeats,
+                                   double* gbs, double* seconds);
+
 // Pattern kernels (ebsd_forward.cu).
 // CTAs that launch_forward would start for p under cfg.
 int64_t forward_ctas(const FwdParams& p, const LaunchCfg& cfg);
-cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s);
-cudaError_t launch_cells(const FwdParams& p, int NV, cudaStream_t s);
+// cells: the diagnostic instantiation that also stores p.nix/niy/ixy0/ixy1.
+cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s,
+                           bool cells = false);
 cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
                                    unsigned long long* counter, int NV, bool noise, int ty,
                                    int grid, cudaStream_t s);

@@ -1,7 +1,12 @@
 // The CTEMEBSD program on the GPU: CTEMEBSD.f90:87-672 end to end, with the
 // pattern loop replaced by libebsdgpu calls and the output written by a
-// writer thread while the next chunk of patterns is computed.
+// writer thread while the next chunk of patterns is computed.  On several
+// GPUs the orientation loop (:573) is split into contiguous shards, one per
+// device and host thread, and every shard writes its records at their own
+// offsets in the one output file (:654-658).
 #include <cuda_runtime.h>
+#include <fcntl.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <chrono>
@@ -41,7 +46,177 @@ int fail(int code, const std::string& msg)
 
 }  // namespace
 
+namespace {
+
+// Positional writer of the output file: the header record, then one
+// gfortran sequential record per pattern at the offset its index gives, so
+// that shards on several GPUs write their records concurrently (pwrite on
+// one descriptor) and the file equals the sequential one byte for byte.
+class RecordFile {
+public:
+    static constexpr size_t kMaxSub = 2147483639u;  // gfortran's largest sub-record
+
+    RecordFile(const char* path, size_t rec_bytes, long long keep_records)
+        : rec_(rec_bytes)
+    {
+        const size_t nsub = rec_bytes == 0 ? 1 : (rec_bytes + kMaxSub - 1) / kMaxSub;
+        per_ = (long long)rec_bytes + 8LL * (long long)nsub;
+        if (keep_records > 0) {
+            fd_ = ::open(path, O_RDWR);
+            // drop whatever follows the kept records (a partial or lone record)
+            if (fd_ >= 0 && ::ftruncate(fd_, (off_t)(20 + keep_records * per_)) != 0) {
+                ::close(fd_);
+                fd_ = -1;
+            }
+        } else {
+            fd_ = ::open(path, O_RDWR | O_CREAT | O_TRUNC, 0644);
+        }
+    }
+    ~RecordFile() { close(); }
+    bool ok() const { return fd_ >= 0; }
+    bool write_header(const int32_t hdr[3])
+    {
+        const int32_t m = 12;
+        return put(0, &m, 4) && put(4, hdr, 12) && put(16, &m, 4);
+    }
+    // record k (0-based pattern index) from rec_ bytes at data
+    bool write_record(long long k, const void* data)
+    {
+        long long off = 20 + k * per_;
+        const char* p = (const char*)data;
+        size_t left = rec_;
+        bool first = true;
+        do {
+            const size_t n = left > kMaxSub ? kMaxSub : left;
+            const bool more = left > n;
+            const int32_t head = more ? -(int32_t)n : (int32_t)n;
+            const int32_t tail = first ? (int32_t)n : -(int32_t)n;
+            if (!put(off, &head, 4) || !put(off + 4, p, n) || !put(off + 4 + (long long)n, &tail, 4))
+                return false;
+            off += (long long)n + 8;
+            p += n;
+            left -= n;
+            first = false;
+        } while (left > 0);
+        return true;
+    }
+    bool close()
+    {
+        if (fd_ < 0) return true;
+        const bool ok = ::close(fd_) == 0;
+        fd_ = -1;
+        return ok;
+    }
+
+private:
+    bool put(long long off, const void* data, size_t n)
+    {
+        const char* p = (const char*)data;
+        while (n > 0) {
+            const ssize_t w = ::pwrite(fd_, p, n, (off_t)off);
+            if (w <= 0) return false;
+            p += w;
+            off += w;
+            n -= (size_t)w;
+        }
+        return true;
+    }
+    int fd_ = -1;
+    size_t rec_ = 0;
+    long long per_ = 0;
+};
+
+// Complete records at the start of an existing output file with this
+// header: every record's two length markers are checked, because shards
+// written in parallel can leave a later record complete behind a missing
+// one.
+int64_t complete_records(const char* path, const int32_t hdr[3], size_t rec, int64_t numeuler)
+{
+    FILE* f = fopen(path, "rb");
+    if (!f) return 0;
+    int32_t head[5] = {0, 0, 0, 0, 0};
+    int64_t done = 0;
+    if (fread(head, 4, 5, f) == 5 && head[0] == 12 && head[4] == 12 && head[1] == hdr[0] &&
+        head[2] == hdr[1] && head[3] == hdr[2]) {
+        const long long per = 4LL * (long long)rec + 8;
+        for (; done < numeuler; ++done) {
+            const long long off = 20 + done * per;
+            int32_t m1 = 0, m2 = 0;
+            if (fseeko(f, (off_t)off, SEEK_SET) != 0 || fread(&m1, 4, 1, f) != 1 ||
+                m1 != (int32_t)(4 * rec) ||
+                fseeko(f, (off_t)(off + 4 + 4LL * (long long)rec), SEEK_SET) != 0 ||
+                fread(&m2, 4, 1, f) != 1 || m2 != m1)
+                break;
+        }
+    }
+    fclose(f);
+    return done;
+}
+
+// One GPU's shard [begin, end): patterns in chunks into a pinned double
+// buffer, each chunk's records written by a writer thread while the next
+// chunk is computed.
+int run_shard(ebsd_handle* h, int device, const float* quats, int64_t begin, int64_t end,
+              const ebsd_epilogue* epi, size_t rec, RecordFile* out, std::string* err)
+{
+    if (begin >= end) return EBSD_OK;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        *err = "cudaSetDevice failed";
+        return EBSD_ECUDA;
+    }
+    const int64_t n = end - begin;
+    const int64_t chunk = std::max<int64_t>(
+        1, std::min<int64_t>(n, (int64_t)((size_t(256) << 20) / (rec * sizeof(float)))));
+    PinnedGuard pg;
+    for (int b = 0; b < 2; ++b) {
+        if (cudaMallocHost(&pg.p[b], std::max<size_t>(1, chunk * rec) * sizeof(float)) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            *err = "pinned output buffer";
+            return EBSD_ENOMEM;
+        }
+    }
+    std::thread writer;
+    bool write_ok = true;
+    int rc = EBSD_OK;
+    for (int64_t o0 = begin, c = 0; o0 < end; o0 += chunk, ++c) {
+        const int64_t m = std::min(chunk, end - o0);
+        float* buf = pg.p[c & 1];
+        // noise keyed by the pattern's index in the whole list, so that the
+        // records do not depend on the chunk or shard that computes them
+        rc = ebsd_set_option(h, "noise_index_offset", o0);
+        if (!rc) rc = ebsd_forward(h, quats + 4 * o0, m, epi, buf);
+        if (rc) {
+            *err = ebsd_last_error(h);
+            break;
+        }
+        if (writer.joinable()) writer.join();
+        if (!write_ok) break;
+        writer = std::thread([out, &write_ok, buf, m, rec, o0] {
+            for (int64_t k = 0; k < m && write_ok; ++k)                // one record per pattern
+                write_ok = out->write_record(o0 + k, buf + (size_t)k * rec);
+        });
+    }
+    if (writer.joinable()) writer.join();
+    if (rc) return rc;
+    if (!write_ok) {
+        *err = "output file write failed";
+        return EBSD_EIO;
+    }
+    return EBSD_OK;
+}
+
+}  // namespace
+
 extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
+{
+    const int32_t d = device;
+    return ebsd_run_namelist_devices(nmlfile, &d, 1, quiet);
+}
+
+extern "C" int ebsd_run_namelist_devices(const char* nmlfile, const int32_t* devices,
+                                         int32_t ndev, int quiet)
 {
     auto say = [&](const char* fmt, auto... args) {
         if (!quiet) {
@@ -49,6 +224,8 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
             fflush(stdout);
         }
     };
+    if (!devices || ndev < 1 || ndev > 64)
+        return fail(EBSD_EINVAL, "ebsd_run_namelist_devices: 1 to 64 devices");
     say(" CTEMEBSD (GB300): Dynamical EBSD patterns, using precomputed MC and master Lambert "
         "projections\n");
 
@@ -101,30 +278,30 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
     }
     say(" -> completed reading Master EBSD pattern file\n");
 
-    HandleGuard hg;
-    rc = ebsd_create(&hg.h, device);
-    if (rc) return rc;
-    ebsd_handle* h = hg.h;
-    auto herr = [&](int code) {
-        host::global_set_error(code, ebsd_last_error(h));
+    // one handle per listed device (a device listed twice gets two handles
+    // that share one device copy of the master and detector tables)
+    std::vector<HandleGuard> hg(ndev);
+    for (int k = 0; k < ndev; ++k) {
+        rc = ebsd_create(&hg[k].h, devices[k]);
+        if (rc) return rc;
+    }
+    ebsd_handle* h = hg[0].h;
+    auto herr = [&](ebsd_handle* hh, int code) {
+        host::global_set_error(code, ebsd_last_error(hh));
         return code;
     };
     if (dictionary) {
         int64_t cnt = 0;
         rc = ebsd_sample_rfz(h, nml.ncubochoric, nml.pgnum, nullptr, nullptr, 0, &cnt);
-        if (rc) return herr(rc);
+        if (rc) return herr(h, rc);
         quats.resize((size_t)cnt * 4);
         rc = ebsd_sample_rfz(h, nml.ncubochoric, nml.pgnum, nullptr, quats.data(), cnt, &cnt);
-        if (rc) return herr(rc);
+        if (rc) return herr(h, rc);
         host::apply_axisangle(nml.axisangle, quats.data(), cnt);
         numeuler = cnt;
         say(" Cubochoric sampling, %d steps, point group %d: %lld orientations in the "
             "fundamental zone\n", nml.ncubochoric, nml.pgnum, (long long)numeuler);
     }
-    rc = ebsd_set_master(h, srtmp.data(), mh.npx, mh.npy, mh.nE, mh.numset);
-    if (rc) return herr(rc);
-    srtmp.clear();
-    srtmp.shrink_to_fit();
 
     ebsd_geometry g;
     g.L = nml.L;
@@ -135,17 +312,55 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
     g.xpc = nml.xpc;
     g.ypc = nml.ypc;
     g.sig = mc.sig;
-    int32_t num_el = 0;
-    rc = ebsd_set_detector(h, &g, accum_e.data(), nsx, nsy, mc.numEbins, Emin, Emax, &num_el);
-    if (rc) return herr(rc);
+    // set-up on every distinct device, concurrently
+    std::vector<int> first(ndev);
+    for (int k = 0; k < ndev; ++k) {
+        first[k] = k;
+        for (int j = 0; j < k; ++j)
+            if (devices[j] == devices[k]) {
+                first[k] = j;
+                break;
+            }
+    }
+    std::vector<int> src_rc(ndev, EBSD_OK);
+    std::vector<int32_t> num_els(ndev, 0);
+    {
+        std::vector<std::thread> th;
+        for (int k = 0; k < ndev; ++k) {
+            if (first[k] != k) continue;
+            th.emplace_back([&, k] {
+                ebsd_handle* hk = hg[k].h;
+                int r = ebsd_set_master(hk, srtmp.data(), mh.npx, mh.npy, mh.nE, mh.numset);
+                if (!r)
+                    r = ebsd_set_detector(hk, &g, accum_e.data(), nsx, nsy, mc.numEbins, Emin,
+                                          Emax, &num_els[k]);
+                src_rc[k] = r;
+            });
+        }
+        for (auto& t : th) t.join();
+    }
+    for (int k = 0; k < ndev; ++k)
+        if (first[k] == k && src_rc[k]) return herr(hg[k].h, src_rc[k]);
+    for (int k = 0; k < ndev; ++k) {
+        if (first[k] == k) continue;
+        rc = ebsd_share_detector(hg[k].h, hg[first[k]].h);
+        if (rc) return herr(hg[k].h, rc);
+        num_els[k] = num_els[first[k]];
+    }
+    srtmp.clear();
+    srtmp.shrink_to_fit();
     accum_e.clear();
     accum_e.shrink_to_fit();
+    const int32_t num_el = num_els[0];
+    for (int k = 1; k < ndev; ++k)
+        if (num_els[k] != num_el)
+            return fail(EBSD_ECUDA, "devices disagree on num_el");
 
     const double pref = host::prefactor(nml.beamcurrent, nml.dwelltime, num_el);
     {
         std::vector<float> W((size_t)mc.numEbins * g.numsx * g.numsy);
         rc = ebsd_get_detector(h, W.data(), nullptr, nullptr, nullptr);
-        if (rc) return herr(rc);
+        if (rc) return herr(h, rc);
         float wmax = W.empty() ? 0.0f : *std::max_element(W.begin(), W.end());
         say(" intensity prefactor = %.15g\n", pref);
         say(" max accum_e_detector = %.8g\n", wmax);
@@ -165,7 +380,7 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
     epi.seed = (uint64_t)nml.seed;
     int32_t rx = 0, ry = 0;
     rc = ebsd_output_dims(h, &epi, &rx, &ry);
-    if (rc) return herr(rc);
+    if (rc) return herr(h, rc);
 
     // output header (:555-561): binned dimensions whenever binning != 1
     int32_t hdr[3] = {nml.numsx, nml.numsy, (int32_t)numeuler};
@@ -175,70 +390,39 @@ extern "C" int ebsd_run_namelist(const char* nmlfile, int device, int quiet)
     }
     const size_t rec = (size_t)rx * ry;
     // resume: an output file with the same header keeps its complete
-    // records (20-byte header record, then 4*rec + 8 bytes per pattern)
+    // records up to the first incomplete one
     int64_t done = 0;
     if (nml.resume) {
-        FILE* f = fopen(nml.datafile, "rb");
-        if (f) {
-            int32_t head[5] = {0, 0, 0, 0, 0};
-            const bool hok = fread(head, 4, 5, f) == 5 && head[0] == 12 && head[4] == 12 &&
-                             head[1] == hdr[0] && head[2] == hdr[1] && head[3] == hdr[2];
-            fseeko(f, 0, SEEK_END);
-            const long long size = (long long)ftello(f);
-            fclose(f);
-            if (hok) {
-                const long long per = 4LL * (long long)rec + 8;
-                done = std::min<int64_t>(numeuler, (size - 20) / per);
-                while (done > 0) {  // the last counted record must be complete
-                    FILE* g2 = fopen(nml.datafile, "rb");
-                    int32_t m1 = 0, m2 = 0;
-                    const long long off = 20 + (done - 1) * per;
-                    bool ok2 = g2 && fseeko(g2, off, SEEK_SET) == 0 && fread(&m1, 4, 1, g2) == 1 &&
-                               fseeko(g2, off + 4 + 4LL * (long long)rec, SEEK_SET) == 0 &&
-                               fread(&m2, 4, 1, g2) == 1;
-                    if (g2) fclose(g2);
-                    if (ok2 && m1 == (int32_t)(4 * rec) && m2 == m1) break;
-                    --done;
-                }
-                say(" resuming after %lld complete patterns\n", (long long)done);
-            }
-        }
+        done = complete_records(nml.datafile, hdr, rec, numeuler);
+        if (done > 0) say(" resuming after %lld complete patterns\n", (long long)done);
     }
-    std::unique_ptr<host::FortranWriter> outp;
-    if (done > 0)
-        outp.reset(new host::FortranWriter(nml.datafile, 20 + done * (4LL * (long long)rec + 8)));
-    else
-        outp.reset(new host::FortranWriter(nml.datafile));
-    host::FortranWriter& out = *outp;
+    RecordFile out(nml.datafile, rec * sizeof(float), done);
     if (!out.ok()) return fail(EBSD_EIO, std::string("cannot create output file '") + nml.datafile + "'");
-    if (done == 0 && !out.write(hdr, sizeof hdr)) return fail(EBSD_EIO, "output header write failed");
+    if (done == 0 && !out.write_header(hdr)) return fail(EBSD_EIO, "output header write failed");
 
+    // contiguous shards of the remaining orientations, one per handle
     const auto t0 = std::chrono::steady_clock::now();                 // Time_start (:567)
-    const int64_t chunk = std::max<int64_t>(
-        1, std::min<int64_t>(numeuler, (int64_t)((size_t(256) << 20) / (rec * sizeof(float)))));
-    PinnedGuard pg;
-    for (int b = 0; b < 2; ++b) {
-        cudaError_t e = cudaMallocHost(&pg.p[b], std::max<size_t>(1, chunk * rec) * sizeof(float));
-        if (e != cudaSuccess) return fail(EBSD_ENOMEM, "pinned output buffer");
-    }
-    std::thread writer;
-    bool write_ok = true;
-    for (int64_t o0 = done, c = 0; o0 < numeuler; o0 += chunk, ++c) {
-        const int64_t m = std::min(chunk, numeuler - o0);
-        float* buf = pg.p[c & 1];
-        rc = ebsd_forward(h, quats.data() + 4 * o0, m, &epi, buf);
-        if (rc) {
-            if (writer.joinable()) writer.join();
-            return herr(rc);
+    const int64_t left = numeuler - done;
+    std::vector<int> shard_rc(ndev, EBSD_OK);
+    std::vector<std::string> shard_err(ndev);
+    {
+        std::vector<std::thread> th;
+        for (int k = 0; k < ndev; ++k) {
+            const int64_t b = done + left * k / ndev, e = done + left * (k + 1) / ndev;
+            th.emplace_back([&, k, b, e] {
+                shard_rc[k] = run_shard(hg[k].h, devices[k], quats.data(), b, e, &epi, rec, &out,
+                                        &shard_err[k]);
+            });
         }
-        if (writer.joinable()) writer.join();
-        writer = std::thread([&out, &write_ok, buf, m, rec] {
-            for (int64_t k = 0; k < m && write_ok; ++k)                // one record per pattern
-                write_ok = out.write(buf + (size_t)k * rec, rec * sizeof(float));
-        });
+        for (auto& t : th) t.join();
     }
-    if (writer.joinable()) writer.join();
-    if (!write_ok || !out.close()) return fail(EBSD_EIO, "output file write failed");
+    for (int k = 0; k < ndev; ++k)
+        if (shard_rc[k]) {
+            char buf[64];
+            snprintf(buf, sizeof buf, "device %d: ", devices[k]);
+            return fail(shard_rc[k], buf + shard_err[k]);
+        }
+    if (!out.close()) return fail(EBSD_EIO, "output file write failed");
     const double secs =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     say("  Total computation time [s] %.3f\n", secs);                 // Time_stop (:669)

@@ -14,7 +14,9 @@
  *   - Arrays are passed in Fortran (column-major) order, exactly as the
  *     reference declares them; nothing is transposed on the host.
  *   - Pattern pointers may be host (pageable or pinned) or device memory;
- *     the library inspects each pointer.  Pointers are borrowed for the
+ *     the library inspects each pointer.  Device memory must be on the
+ *     handle's GPU (or managed): memory of another GPU is refused with
+ *     EBSD_EINVAL before any launch.  Pointers are borrowed for the
  *     duration of the call only.
  *   - One handle owns one device, one CUDA stream and its device buffers.
  *     A handle is not thread-safe; separate handles may run concurrently.
@@ -114,6 +116,11 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    per SM.
  *   "vjp_tile_y"     CTA height of ebsd_vjp and the Gauss-Newton kernels:
  *                    4 (default) or 8; binning 8 always uses 8.
+ *   "noise_index_offset"  the pattern index of the first orientation of the
+ *                    next calls (default 0): Poisson noise is keyed by (seed,
+ *                    pattern index, pixel), so a caller that computes a long
+ *                    orientation list in pieces sets the piece's start here
+ *                    and gets the noise of one call over the whole list.
  *   "vjp_orient_per_cta"  ebsd_vjp's orientations per CTA, 1..64 (default 8).
  *                    (ebsd_vjp_noalloc keeps 8 and 2, the shape its size
  *                    limit is stated for.)
@@ -153,6 +160,17 @@ int ebsd_share_master(ebsd_handle* dst, const ebsd_handle* src);
 int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const int32_t* accum_e,
                       int32_t nsx, int32_t nsy, int32_t numEbins, int32_t Emin, int32_t Emax,
                       int32_t* num_el);
+
+/* Let handle dst use the detector of src (same device) without setting it
+ * up again: the master, the MC histogram, the energy window, num_el and the
+ * detector tables of CTEMEBSD.f90:416-516 are shared, not copied, so jobs
+ * on one detector geometry that differ only in epilogue (binning, gamma,
+ * prefactor, noise) or orientations pay for one set-up.  A handle that later
+ * changes its geometry (ebsd_set_detector, or ebsd_refine of the pattern
+ * centre) first takes tables of its own, so the others are unaffected;
+ * the shared arrays live until the last handle holding them is destroyed.
+ * dst keeps its own options and launch shape.  No reference counterpart. */
+int ebsd_share_detector(ebsd_handle* dst, const ebsd_handle* src);
 
 /* Energy window of CTEMEBSD.f90:361-367 (1-based bin indices). */
 int ebsd_energy_window(float energymin, float energymax, double Ehistmin, double Ebinsize,
@@ -247,10 +265,14 @@ int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue*
  * cotangent mode) is rejected with EBSD_EUNSUPPORTED; larger batches run as
  * several launches through the array.  The first call on a device looks up
  * the array's device address (a one-time set-up), so make that first call
- * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU (other streams, other threads, other handles) race
- * and must be serialised by the caller.  Work is queued on the handle's
- * stream and the call returns without waiting for it. */
+ * before any stream capture.  That address is kept for the life of the
+ * process: after a cudaDeviceReset of the device (which also ends every
+ * handle on it) this entry point must not be called again.  All calls
+ * share the array: calls whose work overlaps on the GPU (other streams,
+ * other threads, other handles) race and must be serialised by the caller.
+ * Buffers on another GPU than the handle's are refused (EBSD_EINVAL).
+ * Work is queued on the handle's stream and the call returns without
+ * waiting for it. */
 int ebsd_vjp_noalloc(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
                      int32_t mode, const float* data, float* loss, float* grad);
 
@@ -293,12 +315,36 @@ int ebsd_refine(ebsd_handle* h, float* quats, int64_t n, const ebsd_epilogue* e,
                 const float* targets, const ebsd_gn_options* opt, float* loss,
                 ebsd_geometry* geom, int32_t* iterations);
 
+/* ebsd_refine over several handles (one per GPU, or several on one GPU),
+ * each holding a shard of the orientations: quats[k], n[k], targets[k] and
+ * loss[k] (loss may be NULL, or an entry NULL) belong to handle hs[k].  All
+ * handles must hold the same detector geometry.  Every iteration runs the
+ * shards' accumulations concurrently (one host thread each), sums their
+ * 12-number pattern-centre systems in shard order in this process, solves
+ * once and applies the same centre step on every handle -- the one
+ * cross-shard quantity of the refinement, reduced without any collective
+ * library.  No reference counterpart. */
+int ebsd_refine_sharded(ebsd_handle* const* hs, int32_t nh, float* const* quats,
+                        const int64_t* n, const ebsd_epilogue* e, const float* const* targets,
+                        const ebsd_gn_options* opt, float* const* loss, ebsd_geometry* geom,
+                        int32_t* iterations);
+
 /* Lambert cells of the loop (CTEMEBSD.f90:584-598) for n quaternions:
  * nix/niy (grid indices in -npx..npx) and the scaled Lambert coordinates
  * ixy0/ixy1, each [n][numsy][numsx].  Host or device pointers.  For parity
- * checking of the cell indices. */
+ * checking of the cell indices.  The cells are stored by the pattern kernel
+ * itself (its diagnostic instantiation, at the handle's launch shape). */
 int ebsd_cells(ebsd_handle* h, const float* quats, int64_t n, int32_t* nix, int32_t* niy,
                float* ixy0, float* ixy1);
+
+/* The pattern loop (as ebsd_forward) and, from the same kernel launch, the
+ * Lambert cells of every pixel and orientation (as ebsd_cells): out
+ * [n][out_ny][out_nx], nix/niy/ixy0/ixy1 [n][numsy][numsx].  Device
+ * pointers only (quats 16-byte aligned); no Poisson noise.  Asynchronous on
+ * the handle's stream.  Reference: the loop body CTEMEBSD.f90:584-608, whose
+ * cell indices (:593-598) and values (:600-608) it exposes together. */
+int ebsd_forward_cells(ebsd_handle* h, const float* quats, int64_t n, const ebsd_epilogue* e,
+                       float* out, int32_t* nix, int32_t* niy, float* ixy0, float* ixy1);
 
 /* Copy the detector weights accum_e_detector(numEbins,numsx,numsy) (zero
  * outside Emin..Emax) and direction cosines rgx/rgy/rgz(numsx,numsy) to
@@ -412,6 +458,17 @@ int ebsd_run_mc_namelist(const char* nmlfile, int device, int quiet);
  * unless quiet != 0. */
 int ebsd_run_namelist(const char* nmlfile, int device, int quiet);
 
+/* ebsd_run_namelist on several GPUs: the orientation loop of
+ * CTEMEBSD.f90:573-663 is split into ndev contiguous shards, one per listed
+ * device, each run by its own handle and host thread; every shard writes
+ * its records at their offsets 20 + k*(4*nx*ny + 8) in the one output file,
+ * which is byte for byte the single-device file.  A device listed twice
+ * gets two handles sharing one device copy of the master and detector.
+ * Resume (namelist key `resume`) keeps the complete records up to the
+ * first incomplete one.  ndev is 1..64. */
+int ebsd_run_namelist_devices(const char* nmlfile, const int32_t* devices, int32_t ndev,
+                              int quiet);
+
 /* Header of a CTEMMC output file (CTEMMC.f90:262-277). */
 typedef struct {
     int32_t numEbins, numzbins, numsx, numsy;
@@ -471,6 +528,23 @@ int ebsd_read_namelist(const char* path, ebsd_namelist* nml);
  * axis-angle pre-rotation.  Call with quats == NULL to get *n only. */
 int ebsd_read_angle_file(const char* path, const char* eulerconvention,
                          const float axisangle[4], int64_t* n, float* quats);
+
+/* Measured read bandwidth of one level of the memory hierarchy of a device,
+ * in GB/s (best of `repeats` timed launches; CUDA events).  The
+ * denominators of the pattern kernel's roofline: its gather is served by L1
+ * and an L2-resident master, which a copy-based HBM figure does not bound.
+ * No reference counterpart.
+ *   EBSD_BW_L1:  every CTA re-reads its own 16 KB with 128-bit L1-cached loads;
+ *   EBSD_BW_L2:  the grid sweeps `bytes` (e.g. 48 MB, L2-resident) with
+ *                128-bit loads that bypass L1;
+ *   EBSD_BW_HBM: the same sweep over `bytes` larger than L2.
+ * Allocates and frees its own buffer; uses the current device's default
+ * settings and changes none. */
+#define EBSD_BW_L1 1
+#define EBSD_BW_L2 2
+#define EBSD_BW_HBM 3
+int ebsd_measure_bandwidth(int32_t device, int32_t level, int64_t bytes, int32_t repeats,
+                           double* gbs);
 
 #ifdef __cplusplus
 }

@@ -3,20 +3,46 @@ from __future__ import annotations
 
 import numpy as np
 
-# Tolerances: Lambert cells bit-exact except pixels within float rounding
-# of a cell edge (counted); intensities within 1e-5 relative of the FP64
-# re-evaluation and within 1e-4 of the FP32 reference.
+# Gates.  Lambert cells are bit-exact except pixels within float rounding of
+# a cell edge (counted).  Intensities: within 1e-5 relative of the FP64
+# re-evaluation and within 1e-4 of the FP32 reference restatement.
 #
-# "Relative" for a pattern is its relative L2 error.  In the default
-# (reference) arithmetic, single pixels near the Lambert poles differ from
-# FP64 by up to ~1e-4 of the pattern maximum because the reference computes
-# 1 - z in single precision (Lambert.f90:427,430); TOL_PIXEL_REF bounds that
-# pixel-wise error.  The optional accurate Lambert arithmetic removes the
-# cancellation and meets TOL_FP64 pixel-wise.
+# Two error measures per pattern: its relative L2 error, and the pixel-wise
+# max |a - ref| / max |ref| (the largest pixel error against the pattern's
+# scale).  Which arithmetic meets which gate:
+#
+# * reference arithmetic (options weights_fp64 = 0, strict_order = 1): the
+#   GPU repeats the reference's single-precision operations in its order, so
+#   against the FP32 restatement it is within TOL_REF pixel-wise (measured
+#   ~1e-6: only CUDA's atanf differs from the C library's).
+# * accurate Lambert arithmetic (lambert_accurate = 1, with the default
+#   binary64 weights): within TOL_FP64 of FP64 pixel-wise on the 501^2
+#   master (measured 7.4e-6 at 80x60); on the 1001^2 master it meets
+#   TOL_FP64 as relative L2 (2.2e-6) and TOL_PIXEL_REF pixel-wise (8.7e-5,
+#   the same pixel error as the default): a single-precision Lambert
+#   coordinate near |ixy| = 500 resolves 3e-5 of a cell (one ulp), so a
+#   few ulps of binary32 geometry move a pixel on a sharp band edge by
+#   ~1e-4 of the pattern maximum whatever 1 - z is computed as.
+# * the default (binary64 weights, the reference's 1 - z): within TOL_FP64
+#   of FP64 as relative L2 and TOL_PIXEL_REF pixel-wise.  Single pixels near
+#   the Lambert poles differ from FP64 by up to ~1e-4 of the pattern maximum
+#   because the reference computes 1 - z in single precision
+#   (Lambert.f90:427,430), which the default keeps so that its cells stay
+#   the reference's.  Against the FP32 restatement the default is within
+#   TOL_REF as relative L2; pixel-wise it differs by the reference's own
+#   single-precision weight error (~1e-4 on sparse MC histograms), which the
+#   binary64 weights do not have.
 TOL_FP64 = 1e-5
 TOL_REF = 1e-4
 TOL_PIXEL_REF = 1e-4
 EDGE_ULPS = 4
+# The binary32 adjoint against the oracle's binary64 analytic gradient: the
+# largest error of each kind (rotation, xpc, ypc, L) relative to the largest
+# component of that kind over the batch.
+TOL_GRAD = 1e-4     # measured <= 8.7e-6 on the small detectors
+TOL_GRAD_C4 = 6e-4  # 480x480 on the 1001^2 master: measured 6.3e-5 (rotation)
+# The loss 1 - <O,T>/(|O||T|) against the binary64 loss, relative.
+TOL_LOSS = 1e-4
 
 
 def rel_errors(a: np.ndarray, ref: np.ndarray):

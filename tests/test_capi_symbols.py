@@ -64,6 +64,13 @@ def test_errors_without_side_effects(built):
         assert len(lib.ebsd_last_error(None)) > 0
     rc = lib.ebsd_create(C.byref(h), 10_000)
     assert rc in (capi.EBSD_ECUDA, capi.EBSD_EINVAL)
+    # the bandwidth probe checks its arguments before any CUDA call
+    v = C.c_double()
+    assert lib.ebsd_measure_bandwidth(0, 9, 1 << 20, 3, C.byref(v)) == capi.EBSD_EINVAL
+    assert lib.ebsd_measure_bandwidth(0, capi.BW_L2, 1 << 20, 0, C.byref(v)) == capi.EBSD_EINVAL
+    assert lib.ebsd_measure_bandwidth(0, capi.BW_L2, 1 << 20, 3, None) == capi.EBSD_EINVAL
+    assert lib.ebsd_measure_bandwidth(10_000, capi.BW_L2, 1 << 20, 3, C.byref(v)) == \
+        capi.EBSD_EINVAL
 
 
 def test_cli_help_and_template(built, tmp_path):

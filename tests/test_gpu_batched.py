@@ -184,3 +184,69 @@ def test_batched_large_jobs_run_as_own_launches(built):
         out.fill_(-1.0)
     capi.Handle(0).forward_batched(jobs, graph=True, queue_all=True)
     check("queue only")
+
+
+@pytest.mark.parametrize("weights", ["fp64", "reference"])
+def test_c3_shaped_jobs_against_the_oracle(built, weights):
+    """Jobs shaped like the 64-job batched workload, run by ebsd_forward_batched
+    and compared with the oracle itself (not with per-job launches): a
+    1244x1024 detector binned 8x8, whose 1244 columns are not whole blocks
+    (the record is cropped to 155 x 128, CTEMEBSD.f90:630-651); the hcp Ti
+    master at half-width 500 on 640x480 binned 2; a one-orientation job; an
+    unbinned 160x120 job.  Once as the default hybrid batch and once with
+    every job through the persistent queue kernel.  With binary64 weights
+    the records are gated against the FP64 re-evaluation; with the
+    reference's single-precision weights against the FP32 restatement."""
+    torch = pytest.importorskip("torch")
+    from oracle import oracle as O
+    from tests.conftest import workload_data
+    from tests.parity import TOL_FP64, TOL_PIXEL_REF, TOL_REF, rel_errors
+    masters = {}
+    for ph in ("Ni", "Ti"):
+        wl = synth.c3_phase(ph)
+        sr, acc = workload_data(wl)
+        mh = capi.Handle(0)
+        mh.set_master(sr)
+        masters[ph] = (mh, sr, acc)
+    specs = [(1244, 1024, 8, "gam", 3, "Ni"), (640, 480, 2, "lin", 4, "Ti"),
+             (80, 60, 4, "gam", 1, "Ti"), (160, 120, 1, "not", 2, "Ni")]
+    jobs, refs = [], []
+    for j, (nx, ny, b, mode, n, ph) in enumerate(specs):
+        mh, sr, acc = masters[ph]
+        h = capi.Handle(0)
+        h.set_option("weights_fp64", int(weights == "fp64"))
+        h.share_master(mh)
+        geom = dict(L=15000.0, thetac=10.0, delta=12800.0 / nx, numsx=nx, numsy=ny, xpc=0.0,
+                    ypc=0.0, sig=70.0)
+        num_el = h.set_detector(geom, acc, 1, 11)
+        pref = capi.prefactor(15.0, 100.0, num_el)
+        epi = capi.epilogue(pref, binning=b, scalingmode=mode, gammavalue=0.33)
+        ox, oy = h.output_dims(epi)
+        assert (ox, oy) == ((nx // b, ny // b) if mode != "not" else (nx, ny))
+        qn = synth.shoemake_quaternions(n, 1000 + j)
+        det = O.Detector(geom, acc, 1, 11)
+        assert det.num_el == num_el
+        m = capi.SCALING[mode]
+        if weights == "fp64":
+            raw = det.patterns_f64(sr, qn, pref, nthreads=O.max_threads())
+            ref = np.stack([O.epilogue_f64(p, b, m, 0.33) for p in raw])
+        else:
+            raw = det.patterns_f32(sr, qn, pref, nthreads=O.max_threads())
+            ref = np.stack([O.epilogue_f32(p, b, m, 0.33) for p in raw])
+        assert ref.shape == (n, oy, ox)
+        jobs.append((h, torch.from_numpy(qn).cuda(),
+                     epi, torch.full((n, oy, ox), -1.0, device="cuda")))
+        refs.append(ref)
+    for queue_all in (False, True):
+        for *_, out in jobs:
+            out.fill_(-1.0)
+        capi.Handle(0).forward_batched(jobs, graph=True, queue_all=queue_all)
+        torch.cuda.synchronize()
+        for (h, q, epi, out), ref, sp in zip(jobs, refs, specs):
+            l2, mx = rel_errors(out.cpu().numpy(), ref)
+            print(weights, "queue_all" if queue_all else "hybrid", sp,
+                  "relL2 %.3g pixel %.3g" % (l2.max(), mx.max()))
+            if weights == "fp64":
+                assert l2.max() <= TOL_FP64 and mx.max() <= TOL_PIXEL_REF, sp
+            else:
+                assert l2.max() <= TOL_REF and mx.max() <= TOL_REF, sp

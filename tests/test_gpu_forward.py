@@ -103,34 +103,67 @@ def test_reference_order_binning(built, binning):
     h.close()
 
 
+def _three_modes(wl, q, n_f32=None):
+    """Patterns of one workload in the three arithmetic modes and the oracle's
+    FP64 and FP32 patterns.  The default mode's patterns and cells come from
+    one launch of the pattern kernel (its cells instantiation), checked bit
+    for bit against the plain launch that the bench times."""
+    O = _oracle()
+    h, det, sr, num_el = _setup(wl)
+    assert num_el == det.num_el
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    epi = capi.epilogue(pref)
+    out, cells = h.forward_cells(q, epi)
+    assert np.array_equal(out, h.forward(q, epi))
+    rep = cell_report(cells, det.cells(q, wl.npx), wl.npx, wl.npx)
+    h.set_option("lambert_accurate", 1)
+    acc_out = h.forward(q, epi)
+    h.close()
+    # reference arithmetic: single-precision weights, reference summation order
+    hr, detr, _, num_el_r = _setup(wl, fp64=False)
+    hr.set_option("strict_order", 1)
+    assert num_el_r == num_el
+    ref_out = hr.forward(q, epi)
+    hr.close()
+    nt = O.max_threads()
+    p64 = det.patterns_f64(sr, q, pref, nthreads=nt)
+    p32 = det.patterns_f32(sr, q, pref, nthreads=nt)
+    return dict(default=out, accurate=acc_out, reference=ref_out, p64=p64, p32=p32, cells=rep,
+                pref=pref, det=det, sr=sr)
+
+
+def _gate_three_modes(tag, r, accurate_pixel=TOL_FP64):
+    print(tag, "cells", r["cells"])
+    assert r["cells"]["non_edge"] == 0, r["cells"]
+    l2, mx = rel_errors(r["default"], r["p64"])
+    print(tag, "default vs FP64: relL2 %.3g pixel %.3g" % (l2.max(), mx.max()))
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_PIXEL_REF
+    l2, mx = rel_errors(r["default"], r["p32"])
+    print(tag, "default vs FP32 reference: relL2 %.3g pixel %.3g" % (l2.max(), mx.max()))
+    assert l2.max() <= TOL_REF
+    l2, mx = rel_errors(r["reference"], r["p32"])
+    print(tag, "reference arithmetic vs FP32 reference: relL2 %.3g pixel %.3g"
+          % (l2.max(), mx.max()))
+    assert l2.max() <= TOL_REF and mx.max() <= TOL_REF
+    l2, mx = rel_errors(r["accurate"], r["p64"])
+    print(tag, "accurate vs FP64: relL2 %.3g pixel %.3g" % (l2.max(), mx.max()))
+    assert l2.max() <= TOL_FP64 and mx.max() <= accurate_pixel
+
+
 def test_c1_parity(built):
-    """80x60 detector, 501^2 x 11 master, 100 orientations, gamma 0.33."""
+    """80x60 detector, 501^2 x 11 master, all 100 orientations: cells from the
+    pattern kernel, the three arithmetic modes against the oracle pixel by
+    pixel, and the gamma epilogue."""
     O = _oracle()
     wl = synth.C1
-    h, det, sr, num_el = _setup(wl)
     q = wl.quaternions()
-    assert num_el == det.num_el
-    rep = cell_report(h.cells(q), det.cells(q, wl.npx), wl.npx, wl.npx)
-    print("C1 cells", rep)
-    assert rep["non_edge"] == 0, rep
-    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
-    raw = h.forward(q, capi.epilogue(pref))
-    p64 = det.patterns_f64(sr, q, pref, nthreads=O.max_threads())
-    p32 = det.patterns_f32(sr, q, pref, nthreads=O.max_threads())
-    l2, mx = rel_errors(raw, p64)
-    print("C1 vs FP64: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
-    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_PIXEL_REF
-    l2, mx = rel_errors(raw, p32)
-    print("C1 vs FP32 reference: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
-    assert l2.max() <= TOL_REF and mx.max() <= 10 * TOL_REF
-    gam = h.forward(q, capi.epilogue(pref, scalingmode="gam", gammavalue=wl.gammavalue))
-    ref = np.stack([O.epilogue_f64(p, 1, 2, wl.gammavalue) for p in p64])
+    r = _three_modes(wl, q)
+    _gate_three_modes("C1", r)
+    h, det, sr, num_el = _setup(wl)
+    gam = h.forward(q, capi.epilogue(r["pref"], scalingmode="gam", gammavalue=wl.gammavalue))
+    ref = np.stack([O.epilogue_f64(p, 1, 2, wl.gammavalue) for p in r["p64"]])
     l2, mx = rel_errors(gam, ref)
     assert l2.max() <= TOL_FP64 and mx.max() <= TOL_PIXEL_REF
-    h.set_option("lambert_accurate", 1)
-    l2, mx = rel_errors(h.forward(q, capi.epilogue(pref)), p64)
-    print("C1 accurate vs FP64: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
-    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64
     h.close()
 
 
@@ -271,34 +304,43 @@ def test_call_order_and_mismatch_errors(built):
     h.close()
 
 
-def test_c2_subset_and_properties(built):
-    """640x480 detector, 1001^2 x 11 master: parity on a subset of the
-    10 000 orientations, plus size-independent properties on more."""
-    O = _oracle()
+def test_c2_parity_64_orientations(built):
+    """640x480 detector, 1001^2 x 11 master: the first 64 of the 10 000
+    orientations in the three arithmetic modes against the oracle pixel by
+    pixel, Lambert cells of all 64 x 307 200 pixel-orientations read out of
+    the pattern kernel, and size-independent properties on the batch."""
     wl = synth.C2
-    h, det, sr, num_el = _setup(wl)
-    assert num_el == det.num_el
     q = wl.quaternions(64)
-    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
-    epi = capi.epilogue(pref)
-    out = h.forward(q, epi)
-    sel = np.arange(0, 64, 8)
-    p64 = det.patterns_f64(sr, q[sel], pref, nthreads=O.max_threads())
-    l2, mx = rel_errors(out[sel], p64)
-    print("C2 vs FP64: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
-    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_PIXEL_REF
-    p32 = det.patterns_f32(sr, q[sel[:2]], pref, nthreads=O.max_threads())
-    l2, mx = rel_errors(out[sel[:2]], p32)
-    # pixel maxima against the FP32 reference carry its single-precision
-    # weight noise (~1e-4 on sparse histograms); the pattern error is gated
-    print("C2 vs FP32 reference: relL2 %.3g max/max %.3g" % (l2.max(), mx.max()))
-    assert l2.max() <= TOL_REF and mx.max() <= 10 * TOL_REF
-    rep = cell_report(h.cells(q[:4]), det.cells(q[:4], wl.npx), wl.npx, wl.npx)
-    print("C2 cells", rep)
-    assert rep["non_edge"] == 0
+    r = _three_modes(wl, q)
+    # on the 1001^2 master a binary32 Lambert coordinate resolves 3e-5 of a
+    # cell, so the accurate mode meets 1e-5 of FP64 as relative L2 only
+    _gate_three_modes("C2", r, accurate_pixel=TOL_PIXEL_REF)
+    assert r["cells"]["pixels"] == 64 * wl.numsx * wl.numsy
     # q and -q, and repeat determinism, on the whole batch
-    assert np.array_equal(out, h.forward(-q, epi))
-    assert np.array_equal(out, h.forward(q, epi))
+    h, det, sr, num_el = _setup(wl)
+    epi = capi.epilogue(r["pref"])
+    assert np.array_equal(r["default"], h.forward(-q, epi))
+    assert np.array_equal(r["default"], h.forward(q, epi))
+    h.close()
+
+
+def test_forward_cells_match_at_every_launch_shape(built):
+    """The cells instantiation stores the same cells and patterns whatever
+    the launch shape (tile height, orientations per CTA, binning)."""
+    O = _oracle()
+    wl = synth.tiny(seed=3, numsx=100, numsy=70, npx=60, nE=6, mc_nsx=80, n_orient=21)
+    h, det, sr, num_el = _setup(wl)
+    q = wl.quaternions()
+    ocells = det.cells(q, wl.npx)
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    for ty, oc, b in ((4, 1, 1), (8, 4, 2), (16, 64, 4), (4, 8, 8)):
+        h.set_option("tile_y", ty)
+        h.set_option("orient_per_cta", oc)
+        epi = capi.epilogue(pref, binning=b, scalingmode="lin" if b > 1 else "not")
+        out, cells = h.forward_cells(q, epi)
+        assert np.array_equal(out, h.forward(q, epi)), (ty, oc, b)
+        rep = cell_report(cells, ocells, wl.npx, wl.npx)
+        assert rep["non_edge"] == 0, (ty, oc, b, rep)
     h.close()
 
 
@@ -368,3 +410,37 @@ def test_binning_8_with_a_four_row_tile(built):
     b = h.forward(q, epi)
     assert np.array_equal(a, b) and np.abs(a).max() > 0
     h.close()
+
+
+def test_shared_detector_matches_own_setup_and_copies_on_write(built):
+    """ebsd_share_detector: a handle on another handle's detector makes the
+    same records as the source; when a holder changes its geometry (a new
+    set-up, or a pattern-centre refinement) it takes tables of its own and
+    the other holders keep theirs; the tables outlive the source handle."""
+    torch = pytest.importorskip("torch")
+    wl = synth.tiny(seed=9, numsx=64, numsy=48, npx=60, nE=5, mc_nsx=80, n_orient=7)
+    sr, acc = workload_data(wl)
+    h, det, _, num_el = _setup(wl)
+    q = wl.quaternions()
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    epi = capi.epilogue(pref, binning=2, scalingmode="gam", gammavalue=0.33)
+    own = h.forward(q, epi)
+    s = capi.Handle(0)
+    s.share_detector(h)
+    assert np.array_equal(s.forward(q, epi), own)
+    # the source moves its pattern centre: the sharing handle is unaffected
+    h.set_detector(dict(wl.geometry(), xpc=wl.xpc + 3.0), acc, 1, wl.nEbins)
+    assert not np.array_equal(h.forward(q, epi), own)
+    assert np.array_equal(s.forward(q, epi), own)
+    h.close()
+    assert np.array_equal(s.forward(q, epi), own)
+    # a second holder, then a pattern-centre refinement on the first
+    s2 = capi.Handle(0)
+    s2.share_detector(s)
+    lin = capi.epilogue(pref)
+    dq = torch.from_numpy(q).cuda()
+    targets = torch.from_numpy(s.forward(q, lin)).cuda()
+    s.refine(dq, lin, targets, max_iterations=2, refine_pc=True)
+    assert np.array_equal(s2.forward(q, epi), own)
+    s.close()
+    s2.close()

@@ -118,3 +118,57 @@ def test_two_phase_api_matches_refine(built):
     h2.refine(b, epi, targets, max_iterations=1, refine_pc=True, damping=1e-3)
     torch.cuda.synchronize()
     assert torch.allclose(a, b, atol=1e-7)
+
+
+def test_sharded_refinement_matches_one_handle(built):
+    """ebsd_refine_sharded: the orientations split over two and three handles
+    (here all on the one GPU; on a node, one per device), their
+    pattern-centre systems summed in this process each iteration, reach the
+    same orientations and centre as ebsd_refine on one handle (the only
+    difference is the order in which the 12-number system is summed)."""
+    torch = pytest.importorskip("torch")
+    wl, h, epi, qt, targets, true_geom = _problem(torch, 1, n=60, pc_shift=(0.5, -0.4, 10.0))
+    rng = np.random.default_rng(5)
+    q0 = perturb(qt, 0.5, rng)
+    start = dict(h.geometry)
+    one = torch.from_numpy(q0).cuda()
+    it1, g1 = h.refine(one, epi, targets, max_iterations=8, refine_pc=True, damping=1e-4,
+                       tol_rad=0.0, tol_pc=0.0)
+    for parts in (2, 3):
+        hs = []
+        for k in range(parts):
+            hk = capi.Handle(0)
+            hk.share_master(h)
+            hk.set_detector(start, wl.mc(), 1, 5)
+            hs.append(hk)
+        cuts = [len(qt) * k // parts for k in range(parts + 1)]
+        qs = [torch.from_numpy(q0[a:b].copy()).cuda() for a, b in zip(cuts, cuts[1:])]
+        ts = [targets[a:b].contiguous() for a, b in zip(cuts, cuts[1:])]
+        losses = [torch.zeros(b - a, device="cuda") for a, b in zip(cuts, cuts[1:])]
+        it, g = capi.refine_sharded(hs, qs, epi, ts, max_iterations=8, refine_pc=True,
+                                    damping=1e-4, tol_rad=0.0, tol_pc=0.0, losses=losses)
+        torch.cuda.synchronize()
+        assert it == it1
+        for k in ("xpc", "ypc", "L"):
+            assert abs(g[k] - g1[k]) < 1e-3, (parts, k, g[k], g1[k])
+        qs_all = torch.cat(qs).cpu().numpy()
+        mis = misorientation_deg(qs_all, one.cpu().numpy())
+        print(parts, "shards: centre", g, "max misorientation to one handle (deg)", mis.max())
+        assert mis.max() < 1e-3
+        assert misorientation_deg(qs_all, qt).max() < 0.01
+        assert all(torch.isfinite(x).all() for x in losses)
+        for hk in hs:
+            assert hk.geometry == g
+            hk.close()
+
+
+def test_sharded_refinement_rejects_mixed_geometries(built):
+    torch = pytest.importorskip("torch")
+    wl, h, epi, qt, targets, true_geom = _problem(torch, 1, n=8)
+    h2 = capi.Handle(0)
+    h2.share_master(h)
+    h2.set_detector(dict(true_geom, xpc=true_geom["xpc"] + 1.0), wl.mc(), 1, 5)
+    q = torch.from_numpy(qt).cuda()
+    with pytest.raises(capi.EBSDError) as e:
+        capi.refine_sharded([h, h2], [q[:4], q[4:]], epi, [targets[:4], targets[4:]])
+    assert e.value.code == capi.EBSD_EINVAL and "geometry" in str(e.value)

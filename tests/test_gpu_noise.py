@@ -72,6 +72,23 @@ def test_poisson_reproducible_and_chunk_independent(built):
     np.testing.assert_allclose(g, ref, rtol=2e-6)
 
 
+def test_noise_index_offset_continues_a_list(built):
+    """Option noise_index_offset: a caller computing a long orientation list
+    in pieces sets each piece's start index and gets the draws of one call
+    over the whole list (noise is keyed by seed, pattern index and pixel)."""
+    wl, h = _setup()
+    q = wl.quaternions(40)
+    epi = capi.epilogue(50.0, poisson=True, seed=9)
+    whole = h.forward(q, epi)
+    h.set_option("noise_index_offset", 17)
+    tail = h.forward(q[17:], epi)
+    h.set_option("noise_index_offset", 0)
+    assert np.array_equal(tail, whole[17:])
+    assert not np.array_equal(h.forward(q[17:], epi), whole[17:])
+    with pytest.raises(capi.EBSDError):
+        h.set_option("noise_index_offset", -1)
+
+
 @pytest.mark.parametrize("lam", [12.5, 27.0, 29.5, 34.0, 340.0, 2.0e4, 1.0e6])
 def test_poisson_distribution_shape(built, lam):
     """The whole distribution, not only its moments: a uniform master with

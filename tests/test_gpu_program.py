@@ -133,3 +133,42 @@ def test_dictionary_run(built, tmp_path):
     ref = det.patterns_f32(sr, q, O.prefactor(15.0, 100.0, det.num_el))
     l2, _ = rel_errors(out, ref)
     assert l2.max() <= TOL_REF
+
+
+@pytest.mark.parametrize("over", [dict(), dict(binning=1, scalingmode="not", poisson=True,
+                                                seed=5)], ids=["gam-bin2", "noise"])
+def test_device_list_writes_the_same_file(built, tmp_path, over):
+    """The orientations split over a device list -- here the one GPU listed
+    two and three times: two or three handles and host threads writing
+    their shards' records concurrently at their offsets -- give the
+    single-device file byte for byte, Poisson noise included (keyed by each
+    pattern's index in the whole list); also through the CLI's -d list."""
+    _inputs(tmp_path, **over)
+    capi.run_namelist(tmp_path / "run.nml", device=0)
+    a = (tmp_path / "out.data").read_bytes()
+    for devs in ([0, 0], [0, 0, 0]):
+        (tmp_path / "out.data").unlink()
+        capi.run_namelist(tmp_path / "run.nml", device=devs)
+        assert (tmp_path / "out.data").read_bytes() == a, devs
+    (tmp_path / "out.data").unlink()
+    exe = capi.LIB_PATH.parent / "ctemebsd"
+    r = subprocess.run([str(exe), "-d", "0,0", str(tmp_path / "run.nml")], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "out.data").read_bytes() == a
+
+
+def test_resume_after_a_shard_stopped_early(built, tmp_path):
+    """A sharded run interrupted with a record missing in the middle (one
+    shard stopped, a later shard went on): resume recomputes from the first
+    incomplete record and the file equals the uninterrupted one."""
+    _inputs(tmp_path)
+    capi.run_namelist(tmp_path / "run.nml", device=[0, 0])
+    full = (tmp_path / "out.data").read_bytes()
+    rec = 4 * 32 * 24 + 8
+    broken = bytearray(full)
+    broken[20 + 3 * rec:20 + 4 * rec] = bytes(rec)   # record 3 never written
+    (tmp_path / "out.data").write_bytes(bytes(broken))
+    _inputs(tmp_path, resume=True)
+    capi.run_namelist(tmp_path / "run.nml", device=[0, 0])
+    assert (tmp_path / "out.data").read_bytes() == full

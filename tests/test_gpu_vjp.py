@@ -7,16 +7,14 @@ import pytest
 
 from ctemsoft_gb300 import capi, synth
 from tests.conftest import workload_data
+from tests.parity import TOL_GRAD, TOL_GRAD_C4, TOL_LOSS
 
 pytestmark = pytest.mark.gpu
 
-# FP32 adjoint against the FP64 analytic gradient: error relative to the
-# largest gradient component of the same kind over the batch.
-TOL_GRAD = 2e-3
 # against central differences at h = 1e-4 rad / 1e-3 px / 1e-2 um: the
 # bilinear interpolation has kinks at cell edges, which the finite
-# difference averages over
-TOL_FD = 2e-2
+# difference averages over (measured 1.1e-3 and 1.4e-3)
+TOL_FD = 1e-2
 
 
 def _grad_err(g, ref):
@@ -62,7 +60,7 @@ def test_ndp_matches_fp64_analytic(built, binning):
     mode = "lin" if binning > 1 else "not"
     loss, g = h.vjp(q, capi.epilogue(pref, binning=binning, scalingmode=mode), T, "ndp")
     rloss, rg = O.vjp_f64(wl.geometry(), acc, 1, wl.nEbins, sr, q, pref, binning, "ndp", T)
-    np.testing.assert_allclose(loss, rloss, rtol=1e-3, atol=1e-6)
+    np.testing.assert_allclose(loss, rloss, rtol=TOL_LOSS, atol=1e-7)
     err = _grad_err(g, rg)
     print("binning", binning, "grad rel err (rot, xpc, ypc, L):", err)
     assert (err < TOL_GRAD).all(), err
@@ -83,8 +81,9 @@ def test_ragged_detector_matches_fp64_analytic(built, binning):
     mode = "lin" if binning > 1 else "not"
     loss, g = h.vjp(q, capi.epilogue(pref, binning=binning, scalingmode=mode), T, "ndp")
     rloss, rg = O.vjp_f64(wl.geometry(), acc, 1, wl.nEbins, sr, q, pref, binning, "ndp", T)
-    np.testing.assert_allclose(loss, rloss, rtol=1e-3, atol=1e-6)
+    np.testing.assert_allclose(loss, rloss, rtol=TOL_LOSS, atol=1e-7)
     err = _grad_err(g, rg)
+    print("ragged binning", binning, "grad rel err (rot, xpc, ypc, L):", err)
     assert (err < TOL_GRAD).all(), err
     h.close()
 
@@ -100,6 +99,7 @@ def test_cotangent_matches_fp64_analytic(built):
     _, g = h.vjp(q, capi.epilogue(pref), cot, "cot")
     _, rg = O.vjp_f64(wl.geometry(), acc, 1, wl.nEbins, sr, q, pref, 1, "cot", cot)
     err = _grad_err(g, rg)
+    print("cotangent grad rel err (rot, xpc, ypc, L):", err)
     assert (err < TOL_GRAD).all(), err
     h.close()
 
@@ -198,10 +198,10 @@ def test_adjoint_480x480_npx500(built):
     T = np.stack(T).astype(np.float32)
     loss, g = h.vjp(q, capi.epilogue(pref), T, "ndp")
     rloss, rg = O.vjp_f64(wl.geometry(), acc, 1, wl.nEbins, sr, q, pref, 1, "ndp", T)
-    np.testing.assert_allclose(loss, rloss, rtol=1e-3)
+    np.testing.assert_allclose(loss, rloss, rtol=TOL_LOSS)
     err = _grad_err(g, rg)
     print("480x480 grad rel err vs FP64 analytic (rot, xpc, ypc, L):", err)
-    assert (err < TOL_GRAD).all(), err
+    assert (err < TOL_GRAD_C4).all(), err
 
     def L(gm, qs):
         P = O.Detector(gm, acc, 1, wl.nEbins).patterns_f64(sr, qs, 1.0,
