@@ -123,6 +123,22 @@ module ebsd_gpu
       integer(c_int), value :: device, quiet
     end function
 
+    ! The program with the orientations split over several devices.
+    integer(c_int) function ebsd_run_namelist_devices(nmlfile, devices, ndev, quiet) &
+        bind(C, name="ebsd_run_namelist_devices")
+      import :: c_int, c_int32_t, c_char
+      character(kind=c_char), intent(in) :: nmlfile(*)  ! NUL-terminated
+      integer(c_int32_t), intent(in) :: devices(*)
+      integer(c_int32_t), value :: ndev
+      integer(c_int), value :: quiet
+    end function
+
+    ! Another handle's master and detector set-up, shared without a copy.
+    integer(c_int) function ebsd_share_detector(dst, src) bind(C, name="ebsd_share_detector")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: dst, src
+    end function
+
     ! The CTEMMC program (&MCdata namelist in, MC file out).
     integer(c_int) function ebsd_run_mc_namelist(nmlfile, device, quiet) &
         bind(C, name="ebsd_run_mc_namelist")
