@@ -452,8 +452,7 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
             return set_err(h, EBSD_ESTATE, "weights_fp64 applies at the next ebsd_set_detector");
     } else if (k == "strict_order") {
         h->cfg.strict = value != 0;
-    } else if (k == "staged_gather") {
-        h->cfg.stage = value != 0;
+
     } else if (k == "l2_persist") {
         if (!value) {
             h->cfg.persist_base = nullptr;
@@ -1513,7 +1512,7 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         b.p.out = J.out;
         b.p.n = J.n;
         if (!(flags & EBSD_BATCH_QUEUE_ALL) &&
-            forward_ctas(b.p, src->NV, src->cfg) >= (int64_t)kBatchLargeCtasPerSm * sms) {
+            forward_ctas(b.p, src->cfg) >= (int64_t)kBatchLargeCtasPerSm * sms) {
             BatchLarge L;
             memset(&L, 0, sizeof L);
             L.p = b.p;

@@ -27,104 +27,6 @@ namespace {
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
-// ---- staged gather ------------------------------------------------------
-// The staged variant copies each tile's master footprint (the nodes its
-// pixels' cells touch for one orientation) into shared memory with bulk
-// copies (cp.async.bulk, completing on an mbarrier) and gathers from there.
-// A quarter-warp's 128-bit global loads cost one L1 wavefront per cache line
-// they touch (about two for the 4 x 2 pixel blocks of the default path);
-// from shared memory they cost one per bank conflict, and the footprint's
-// row pitch is chosen so that neighbouring nodes fall in different banks.
-// Tiles are 16 x 8 pixels: at 640x480 on the 1001^2 master their median
-// footprint is 81 nodes (3.9 KB, 30 bytes per pixel against the 192 bytes
-// per pixel the gather reads); a footprint larger than kStageBytes (a tile
-// across the hemisphere fold) is gathered from global memory instead.
-constexpr int kStageTX = 16, kStageTY = 8;
-constexpr int kStageBytes = 8192;
-// shared-memory layout after the binning scratch of kStageTY x 33 floats
-constexpr int kStageOffFp = 33 * kStageTY * 4;       // int4 per warp: footprint
-constexpr int kStageOffHdr = kStageOffFp + 4 * 16;   // int4 header, int abort flag
-constexpr int kStageOffBar = kStageOffHdr + 32;      // the mbarrier (8 bytes)
-constexpr int kStageOffBuf = (kStageOffBar + 8 + 127) / 128 * 128;
-constexpr int kStageSmem = kStageOffBuf + kStageBytes;
-static_assert(kStageOffFp % 16 == 0 && kStageOffBar % 8 == 0, "shared-memory alignment");
-// try_wait rounds before a wait gives up (each round may suspend the
-// thread for a while; far beyond any copy's latency)
-constexpr unsigned kStageWaitRounds = 1u << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-
-// One bulk copy global -> this CTA's shared memory, counted on bar.  dst,
-// src and bytes are multiples of 16 (nodes are NV x 16 bytes).
-__device__ __forceinline__ void bulk_to_smem(uint32_t dst, const void* src, uint32_t bytes,
-                                             uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-        ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
-        : "memory");
-}
-
-// Wait for the phase of bar with this parity; false if it did not complete
-// within kStageWaitRounds rounds.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
-{
-    for (unsigned i = 0; i < kStageWaitRounds; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-// Row pitch (in nodes) of a staged footprint fw nodes wide: the smallest
-// pitch >= fw with NV * pitch = 4 (mod 8) float4, so that node (x, y + 1)
-// is four 16-byte bank groups away from (x, y) and its neighbours three
-// and seven (odd NV); every NV not a multiple of 8 has one.
-template <int NV>
-__device__ __forceinline__ int stage_pitch(int fw)
-{
-    int pitch = fw;
-    if (NV % 8 != 0)
-        while ((NV * pitch) % 8 != 4) ++pitch;
-    return pitch;
-}
-
-}  // namespace
-
-// CTAs of the staged variant whose bounded waits gave up (an error the host
-// reads back with forward_stage_timeouts); never expected.
-__device__ unsigned int g_stage_timeouts;
-
-namespace {
-
-template <bool SMEM>
-__device__ __forceinline__ float4 ld4(const float4* p, uint64_t pol)
-{
-    if (SMEM) return *p;  // a shared-memory footprint (after the copies' barrier)
-    return ldg4_keep(p, pol);
-}
-
 // 'gam' scaling, pattern**gammavalue (CTEMEBSD.f90:647-649).  The
 // reference-order variant (STRICT) calls powf; the default takes the
 // hardware exp2/log2 form (__powf, a few ulps) for positive values, 6 % of
@@ -144,9 +46,7 @@ __device__ __forceinline__ float gamma_pow(float x, float g)
 // products of the weights with the four corner vectors, each accumulated
 // with fused multiply-adds, then combined with the bilinear corner weights:
 // about a third of the arithmetic, and no less accurate.
-// SMEM: master is the staged footprint in shared memory (gx its pitch,
-// indices relative to the footprint's corner).
-template <int NV, bool STRICT, bool SMEM = false>
+template <int NV, bool STRICT>
 __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master, int gx,
                                               int ix0, int iy0, int ix1, int iy1, float dx,
                                               float dy, const float4 (&w)[NV], uint64_t pol)
@@ -162,8 +62,8 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
         float acc = 0.0f;
 #pragma unroll
         for (int c = 0; c < NV; ++c) {
-            const float4 a = ld4<SMEM>(m00 + c, pol), b = ld4<SMEM>(m10 + c, pol),
-                         e = ld4<SMEM>(m01 + c, pol), f = ld4<SMEM>(m11 + c, pol);
+            const float4 a = ldg4_keep(m00 + c, pol), b = ldg4_keep(m10 + c, pol),
+                         e = ldg4_keep(m01 + c, pol), f = ldg4_keep(m11 + c, pol);
             acc = acc + w[c].x * (a.x * dxm * dym + b.x * dx * dym + e.x * dxm * dy + f.x * dx * dy);
             acc = acc + w[c].y * (a.y * dxm * dym + b.y * dx * dym + e.y * dxm * dy + f.y * dx * dy);
             acc = acc + w[c].z * (a.z * dxm * dym + b.z * dx * dym + e.z * dxm * dy + f.z * dx * dy);
@@ -174,8 +74,8 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
     float c00 = 0.0f, c10 = 0.0f, c01 = 0.0f, c11 = 0.0f;
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
-        const float4 a = ld4<SMEM>(m00 + c, pol), b = ld4<SMEM>(m10 + c, pol),
-                     e = ld4<SMEM>(m01 + c, pol), f = ld4<SMEM>(m11 + c, pol);
+        const float4 a = ldg4_keep(m00 + c, pol), b = ldg4_keep(m10 + c, pol),
+                     e = ldg4_keep(m01 + c, pol), f = ldg4_keep(m11 + c, pol);
         c00 = fmaf(w[c].x, a.x, fmaf(w[c].y, a.y, fmaf(w[c].z, a.z, fmaf(w[c].w, a.w, c00))));
         c10 = fmaf(w[c].x, b.x, fmaf(w[c].y, b.y, fmaf(w[c].z, b.z, fmaf(w[c].w, b.w, c10))));
         c01 = fmaf(w[c].x, e.x, fmaf(w[c].y, e.y, fmaf(w[c].z, e.z, fmaf(w[c].w, e.w, c01))));
@@ -232,15 +132,11 @@ __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, fl
 // each pixel's Lambert cell and coordinates (prm.nix, niy, ixy0, ixy1, one
 // value per orientation and detector pixel) -- a diagnostic instantiation
 // of this template, so that cell parity is read out of the code that makes
-// the patterns.  STAGE: the staged gather (16 x 8 tiles, tile_y must be 8,
-// `tile` the start of kStageSmem bytes of shared memory, every thread of
-// the CTA calls this function).
-template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false,
-          bool STAGE = false>
+// the patterns.
+template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false>
 __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, int tiles_x, int t,
                                              int64_t o_begin, int opc, float* tile, int bw)
 {
-    constexpr int TX = STAGE ? kStageTX : kTileX;  // tile width in pixels
     const int tid = threadIdx.x;
     const bool binned = prm.mode != EBSD_SCALING_NOT && prm.binning > 1;
     const int b = prm.binning;
@@ -253,7 +149,7 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
     // blocks (16 x 2, 8 x 4), which are then summed within the warp.
     if (binned && b <= 4) bw = 32 / b;
     if (BIN8) bw = 8;  // an 8x8 block is two 8 x 4 warps
-    const int bh = 32 / bw, wpr = TX / bw;
+    const int bh = 32 / bw, wpr = kTileX / bw;
     const int lane = tid & 31, wid = tid >> 5;
     int lx = lane % bw, ly = lane / bw;
     if (!binned && bw == 16) {
@@ -264,30 +160,10 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
         ly = (lane >> 2) & 1;
     }
     const int tx = (wid % wpr) * bw + lx, ty = (wid / wpr) * bh + ly;
-    const int x = (t % tiles_x) * TX + tx;
+    const int x = (t % tiles_x) * kTileX + tx;
     const int y = (t / tiles_x) * tile_y + ty;
     const bool inside = x < prm.numsx && y < prm.numsy;
     const int p = y * prm.numsx + x;
-
-    // staged gather: the footprint buffer and its mbarrier
-    char* const sbase = reinterpret_cast<char*>(tile);
-    int4* const s_fp = reinterpret_cast<int4*>(sbase + kStageOffFp);
-    int4* const s_hdr = reinterpret_cast<int4*>(sbase + kStageOffHdr);
-    int* const s_abort = reinterpret_cast<int*>(sbase + kStageOffHdr + 16);
-    const float4* const s_buf = reinterpret_cast<const float4*>(sbase + kStageOffBuf);
-    const uint32_t bar = smem_u32(sbase + kStageOffBar);
-    uint32_t phase = 0;   // parity of the mbarrier phase the next copies complete
-    bool waited_ok = true;
-    if (STAGE) {
-        if (tid == 0) {
-            mbar_init(bar, 1);
-            *s_abort = 0;
-            // the barrier's initialisation visible to the bulk copies
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        }
-        __syncthreads();
-    }
 
     const uint64_t pol = l2_policy_evict_last();
     float4 r = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
@@ -306,17 +182,15 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
     if (o_end > prm.n) o_end = prm.n;
     for (int64_t o = o_begin; o < o_end; ++o) {
         float val = 0.0f;
-        int ix0 = 0, iy0 = 0, ix1 = 0, iy1 = 0;
-        float dx = 0.0f, dy = 0.0f;
         if (inside) {
             const float4 q = ldg4(prm.quats + o);
             float ixy0, ixy1;
             pixel_lambert(q, r, prm.scl, prm.spi2, prm.accurate != 0, ixy0, ixy1);
+            float dx, dy;
             int nix, niy;
-            ix0 = lambert_cell(ixy0, prm.npx, dx, nix);
-            iy0 = lambert_cell(ixy1, prm.npy, dy, niy);
-            ix1 = min(ix0 + 1, 2 * prm.npx);
-            iy1 = min(iy0 + 1, 2 * prm.npy);
+            const int ix0 = lambert_cell(ixy0, prm.npx, dx, nix);
+            const int iy0 = lambert_cell(ixy1, prm.npy, dy, niy);
+            const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
             if (CELLS) {
                 const int64_t ci = o * (int64_t)prm.P + p;
                 prm.nix[ci] = nix;
@@ -324,68 +198,8 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
                 prm.ixy0[ci] = ixy0;
                 prm.ixy1[ci] = ixy1;
             }
-        }
-        bool staged = false;
-        int4 hd = make_int4(0, 0, 0, 0);
-        if (STAGE) {
-            // the tile's footprint: node rectangle of all its pixels' corners
-            int lox = inside ? ix0 : 0x7fffffff, hix = inside ? ix1 : -1;
-            int loy = inside ? iy0 : 0x7fffffff, hiy = inside ? iy1 : -1;
-            lox = __reduce_min_sync(0xffffffffu, lox);
-            hix = __reduce_max_sync(0xffffffffu, hix);
-            loy = __reduce_min_sync(0xffffffffu, loy);
-            hiy = __reduce_max_sync(0xffffffffu, hiy);
-            if (lane == 0) s_fp[wid] = make_int4(lox, hix, loy, hiy);
-            // every thread is past its previous gather from the buffer
-            __syncthreads();
-            if (*s_abort) {
-                // a wait gave up: wait (bounded) for this thread's own copies
-                // still in flight, then leave with the rest of the CTA
-                if (tid == 0 && !waited_ok) mbar_wait(bar, phase ^ 1u);
-                return;
-            }
-            if (tid == 0) {
-                int4 f = s_fp[0];
-                for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
-                    const int4 g = s_fp[k];
-                    f.x = min(f.x, g.x);
-                    f.y = max(f.y, g.y);
-                    f.z = min(f.z, g.z);
-                    f.w = max(f.w, g.w);
-                }
-                int ok = f.y >= f.x;  // some pixel inside the detector
-                const int fw = f.y - f.x + 1, fh = f.w - f.z + 1;
-                const int pitch = ok ? stage_pitch<NV>(fw) : 0;
-                ok = ok && (long long)pitch * fh * NV * 16 <= kStageBytes;
-                *s_hdr = make_int4(f.x, f.z, pitch, ok);
-                if (ok) {
-                    // the buffer's previous readers (generic proxy) before
-                    // the copies (async proxy) overwrite it
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    const uint32_t row = (uint32_t)fw * NV * 16;
-                    mbar_expect_tx(bar, row * (uint32_t)fh);
-                    const uint32_t dst = smem_u32(s_buf);
-                    for (int rr = 0; rr < fh; ++rr)
-                        bulk_to_smem(dst + (uint32_t)(rr * pitch * NV * 16),
-                                     prm.master + ((size_t)(f.z + rr) * prm.gx + f.x) * NV, row,
-                                     bar);
-                }
-            }
-            __syncthreads();
-            hd = *s_hdr;
-            staged = hd.w != 0;
-            if (staged) {
-                waited_ok = mbar_wait(bar, phase);
-                phase ^= 1u;
-                if (!waited_ok && atomicExch(s_abort, 1) == 0) atomicAdd(&g_stage_timeouts, 1u);
-            }
-        }
-        if (inside) {
             const float acc =
-                staged ? gather_pixel<NV, STRICT, true>(s_buf, hd.z, ix0 - hd.x, iy0 - hd.y,
-                                                        ix1 - hd.x, iy1 - hd.y, dx, dy, w, pol)
-                       : gather_pixel<NV, STRICT>(prm.master, prm.gx, ix0, iy0, ix1, iy1, dx,
-                                                  dy, w, pol);
+                gather_pixel<NV, STRICT>(prm.master, prm.gx, ix0, iy0, ix1, iy1, dx, dy, w, pol);
             // :608 -- binary64 in the reference order; otherwise one binary32
             // multiply by the prefactor rounded once (within an ulp of the
             // binary64 product; 4 % faster at 640x480 than the slow FP64 pipe)
@@ -404,7 +218,7 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
             if (lane < bw && (lane & (b - 1)) == 0) {                        // top-left lanes
                 s = s * prm.bindx;                                           // :640
                 if (prm.mode == EBSD_SCALING_GAM) s = gamma_pow<STRICT>(s, prm.gammavalue);
-                const int X = ((t % tiles_x) * TX + tx) / b;
+                const int X = ((t % tiles_x) * kTileX + tx) / b;
                 const int Y = ((t / tiles_x) * tile_y + ty) / b;
                 if (X < prm.out_nx && Y < prm.out_ny)
                     __stcs(prm.out + o * rec + (int64_t)Y * prm.out_nx + X, s);
@@ -426,7 +240,7 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
                 float sb = sh + *slot;
                 sb = sb * prm.bindx;                                         // :640
                 if (prm.mode == EBSD_SCALING_GAM) sb = gamma_pow<false>(sb, prm.gammavalue);
-                const int X = ((t % tiles_x) * TX) / 8 + wid % wpr;
+                const int X = ((t % tiles_x) * kTileX) / 8 + wid % wpr;
                 const int Y = ((t / tiles_x) * tile_y) / 8 + (rgrp >> 1);
                 if (X < prm.out_nx && Y < prm.out_ny)
                     __stcs(prm.out + o * rec + (int64_t)Y * prm.out_nx + X, sb);
@@ -434,26 +248,20 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
         } else {
             tile[ty * 33 + tx] = val;
             __syncthreads();
-            const int nbx = TX / b, nby = tile_y / b;
+            const int nbx = kTileX / b, nby = tile_y / b;
             if (tx < nbx && ty < nby) {
                 float s = 0.0f;                                              // :636 sum()
                 for (int jj = 0; jj < b; ++jj)
                     for (int ii = 0; ii < b; ++ii) s = s + tile[(ty * b + jj) * 33 + tx * b + ii];
                 s = s * prm.bindx;                                           // :640
                 if (prm.mode == EBSD_SCALING_GAM) s = gamma_pow<STRICT>(s, prm.gammavalue);
-                const int X = ((t % tiles_x) * TX) / b + tx;
+                const int X = ((t % tiles_x) * kTileX) / b + tx;
                 const int Y = ((t / tiles_x) * tile_y) / b + ty;
                 if (X < prm.out_nx && Y < prm.out_ny)
                     __stcs(prm.out + o * rec + (int64_t)Y * prm.out_nx + X, s);
             }
             __syncthreads();
         }
-    }
-    if (STAGE) {
-        // a wait that gave up on the last orientation: its copies may still
-        // be in flight into this CTA's shared memory
-        __syncthreads();
-        if (*s_abort && tid == 0 && !waited_ok) mbar_wait(bar, phase ^ 1u);
     }
 }
 
@@ -495,16 +303,15 @@ int resolve_opc(int opc, int64_t n, int ntiles)
 #define EBSD_FWD_LAUNCH_BOUNDS __launch_bounds__(512)
 #endif
 
-template <int NV, bool STRICT, bool NOISE, bool BIN8, bool CELLS = false, bool STAGE = false>
+template <int NV, bool STRICT, bool NOISE, bool BIN8, bool CELLS = false>
 __global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y, int tiles_x,
                                                  int ntiles, int opc, int warp_w)
 {
-    // [tile_y][33] floats (binning); STAGE: kStageSmem bytes, see forward_tile
-    extern __shared__ __align__(128) float tile[];
+    extern __shared__ float tile[];  // [tile_y][33], binning only
     const int t = (int)(blockIdx.x % (unsigned)ntiles);
     const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
-    forward_tile<NV, STRICT, NOISE, BIN8, CELLS, STAGE>(prm, tile_y, tiles_x, t, o_begin, opc,
-                                                        tile, warp_w);
+    forward_tile<NV, STRICT, NOISE, BIN8, CELLS>(prm, tile_y, tiles_x, t, o_begin, opc, tile,
+                                                 warp_w);
 }
 
 // Batched pattern loop: one persistent grid works through a queue of work
@@ -583,36 +390,15 @@ __global__ void __launch_bounds__(32 * TY, TY == 4 ? EBSD_BATCH_MIN_BLOCKS4 : 32
     }
 }
 
-// Tile shape of a launch: STAGE takes 16 x 8 tiles, the others 32 x tile_y
-// (raised until binned records hold whole b x b blocks).
-inline void tile_shape(const FwdParams& p, const LaunchCfg& cfg, bool stage, int& tile_x,
-                       int& tile_y)
-{
-    if (stage) {
-        tile_x = kStageTX;
-        tile_y = kStageTY;
-        return;
-    }
-    tile_x = kTileX;
-    tile_y = cfg.tile_y;
-    if (p.mode != EBSD_SCALING_NOT && p.binning > 1)
-        while (tile_y % p.binning != 0 && tile_y < 16) tile_y *= 2;
-}
-
-// The staged gather serves energy windows of 1..7 float4 per node (a
-// multiple of 8 would put every node's k-th vector in the same banks).
-inline bool stage_eligible(int NV, const LaunchCfg& cfg)
-{
-    return cfg.stage && NV <= 7 && cfg.warp_w != 32;
-}
-
-template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false,
-          bool STAGE = false>
+template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false>
 cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
-    int tile_x, tile_y;
-    tile_shape(p, cfg, STAGE, tile_x, tile_y);
-    const int tiles_x = (p.numsx + tile_x - 1) / tile_x;
+    // binned records are summed inside a CTA: its height must hold whole
+    // b x b blocks (binning 8 on a 4-row tile would write nothing)
+    int tile_y = cfg.tile_y;
+    if (p.mode != EBSD_SCALING_NOT && p.binning > 1)
+        while (tile_y % p.binning != 0 && tile_y < 16) tile_y *= 2;
+    const int tiles_x = (p.numsx + kTileX - 1) / kTileX;
     const int tiles_y = (p.numsy + tile_y - 1) / tile_y;
     const int ntiles = tiles_x * tiles_y;
     const int opc = resolve_opc(cfg.orient_per_cta, p.n, ntiles);
@@ -621,41 +407,30 @@ cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3((unsigned)blocks);
-    lc.blockDim = dim3(tile_x * tile_y);
-    lc.dynamicSmemBytes = STAGE ? kStageSmem : sizeof(float) * 33 * tile_y;
+    lc.blockDim = dim3(kTileX * tile_y);
+    lc.dynamicSmemBytes = sizeof(float) * 33 * tile_y;
     lc.stream = s;
     cudaLaunchAttribute attr[1];
     set_persist_attr(cfg, attr, lc);
     const int warp_w = cfg.warp_w == 32 ? 32 : 16;
-    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE, BIN8, CELLS, STAGE>, p, tile_y,
-                              tiles_x, ntiles, opc, warp_w);
-}
-
-template <int NV, bool STAGE>
-cudaError_t launch_nv_s(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s, bool cells)
-{
-    const bool bin8 = !cfg.strict && p.mode != EBSD_SCALING_NOT && p.binning == 8;
-    if (cells)  // the diagnostic instantiations (no noise)
-        return cfg.strict ? launch_nv2<NV, true, false, false, true, STAGE>(p, cfg, s)
-               : bin8     ? launch_nv2<NV, false, false, true, true, STAGE>(p, cfg, s)
-                          : launch_nv2<NV, false, false, false, true, STAGE>(p, cfg, s);
-    if (p.poisson)  // noise: fused gather
-        return bin8 ? launch_nv2<NV, false, true, true, false, STAGE>(p, cfg, s)
-                    : launch_nv2<NV, false, true, false, false, STAGE>(p, cfg, s);
-    if (cfg.strict) return launch_nv2<NV, true, false, false, false, STAGE>(p, cfg, s);
-    return bin8 ? launch_nv2<NV, false, false, true, false, STAGE>(p, cfg, s)
-                : launch_nv2<NV, false, false, false, false, STAGE>(p, cfg, s);
+    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE, BIN8, CELLS>, p, tile_y, tiles_x,
+                              ntiles, opc, warp_w);
 }
 
 template <int NV>
 cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s, bool cells)
 {
-    if constexpr (NV <= 7) {
-        if (stage_eligible(NV, cfg)) {
-            return launch_nv_s<NV, true>(p, cfg, s, cells);
-        }
-    }
-    return launch_nv_s<NV, false>(p, cfg, s, cells);
+    const bool bin8 = !cfg.strict && p.mode != EBSD_SCALING_NOT && p.binning == 8;
+    if (cells)  // the diagnostic instantiations (no noise)
+        return cfg.strict ? launch_nv2<NV, true, false, false, true>(p, cfg, s)
+               : bin8     ? launch_nv2<NV, false, false, true, true>(p, cfg, s)
+                          : launch_nv2<NV, false, false, false, true>(p, cfg, s);
+    if (p.poisson)  // noise: fused gather
+        return bin8 ? launch_nv2<NV, false, true, true>(p, cfg, s)
+                    : launch_nv2<NV, false, true>(p, cfg, s);
+    if (cfg.strict) return launch_nv2<NV, true, false>(p, cfg, s);
+    return bin8 ? launch_nv2<NV, false, false, true>(p, cfg, s)
+                : launch_nv2<NV, false, false>(p, cfg, s);
 }
 
 template <int NV, bool NOISE, int TY>
@@ -731,11 +506,12 @@ int batched_grid(int NV, bool noise, int ty)
     }
 }
 
-int64_t forward_ctas(const FwdParams& p, int NV, const LaunchCfg& cfg)
+int64_t forward_ctas(const FwdParams& p, const LaunchCfg& cfg)
 {
-    int tile_x, tile_y;
-    tile_shape(p, cfg, stage_eligible(NV, cfg), tile_x, tile_y);
-    const int ntiles = ((p.numsx + tile_x - 1) / tile_x) * ((p.numsy + tile_y - 1) / tile_y);
+    int tile_y = cfg.tile_y;
+    if (p.mode != EBSD_SCALING_NOT && p.binning > 1)
+        while (tile_y % p.binning != 0 && tile_y < 16) tile_y *= 2;
+    const int ntiles = ((p.numsx + kTileX - 1) / kTileX) * ((p.numsy + tile_y - 1) / tile_y);
     const int opc = resolve_opc(cfg.orient_per_cta, p.n, ntiles);
     return ((p.n + opc - 1) / opc) * (int64_t)ntiles;
 }
@@ -764,21 +540,6 @@ cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cud
         case 16: return launch_nv<16>(p, cfg, s, cells);
         default: return cudaErrorInvalidValue;
     }
-}
-
-unsigned forward_stage_timeouts(bool reset)
-{
-    unsigned v = 0;
-    if (cudaMemcpyFromSymbol(&v, g_stage_timeouts, sizeof v) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    if (reset && v) {
-        const unsigned z = 0;
-        cudaMemcpyToSymbol(g_stage_timeouts, &z, sizeof z);
-        cudaGetLastError();
-    }
-    return v;
 }
 
 }  // namespace ebsd

@@ -85,7 +85,6 @@ struct LaunchCfg {
     int orient_per_cta = 0;  // 0: chosen per launch from the grid size
     int warp_w = 16;         // pixels along x per warp: 16 (16 x 2) or 32 (32 x 1)
     bool strict = false;   // reference summation order in the gather
-    bool stage = false;    // staged gather: tile footprints copied to shared memory
     // L2 access-policy window kept persisting for the master pattern
     const void* persist_base = nullptr;
     size_t persist_bytes = 0;
@@ -145,10 +144,7 @@ cudaError_t measure_read_bandwidth(int device, int level, long long bytes, int r
 
 // Pattern kernels (ebsd_forward.cu).
 // CTAs that launch_forward would start for p under cfg.
-int64_t forward_ctas(const FwdParams& p, int NV, const LaunchCfg& cfg);
-// CTAs of the staged gather whose bounded wait gave up since the last reset
-// (reads device memory: synchronises the current device's work first).
-unsigned forward_stage_timeouts(bool reset);
+int64_t forward_ctas(const FwdParams& p, const LaunchCfg& cfg);
 // cells: the diagnostic instantiation that also stores p.nix/niy/ixy0/ixy1.
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s,
                            bool cells = false);

@@ -109,12 +109,6 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *   "l2_persist"     0 drops the persisting L2 window that ebsd_set_master
  *                    places on the master (kept by default where the device
  *                    offers one; 1 keeps it, an error if there is none).
- *   "staged_gather"  1: the pattern kernel copies each 16 x 8 pixel tile's
- *                    master footprint into shared memory and gathers from
- *                    there (tiles whose footprint exceeds 8 KB, and energy
- *                    windows of more than 28 bins, gather from global
- *                    memory); the records are bit for bit those of the
- *                    global gather.  0 (default): gather from global memory.
  *   "tile_y"         pattern-kernel CTA height in pixels: 4 (default), 8, 16;
  *                    raised to 8 when the epilogue bins 8x8.
  *   "orient_per_cta" orientations per CTA, 1..64, or 0 (default): 64,
