@@ -320,13 +320,17 @@ __global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y
 // atomic increment and stops when the queue is exhausted -- no CTA waits
 // on another, so nothing can spin.  Jobs are ordered by item_begin.
 // TY is the tile height (CTA = 32 x TY threads); a group's jobs all use it.
-// Both heights get 1024 resident threads per SM at up to 64 registers
-// (EBSD_BATCH_MIN_BLOCKS4: resident 32 x 4 CTAs the register budget allows).
+// Noise-free 32 x 4 CTAs are held to 56 registers, so that nine are resident
+// per SM as for the per-job pattern kernel (55 registers): with eight (64
+// registers) every job of the 64-job workload through the queue ran at
+// 268.1 k patterns/s, with nine at 272.1 k.  The noise variant keeps eight
+// (its sampler spills at 56 registers); 32 x 8 CTAs get 1024 threads per SM.
 #ifndef EBSD_BATCH_MIN_BLOCKS4
-#define EBSD_BATCH_MIN_BLOCKS4 8
+#define EBSD_BATCH_MIN_BLOCKS4 9
 #endif
 template <int NV, bool NOISE, int TY>
-__global__ void __launch_bounds__(32 * TY, TY == 4 ? EBSD_BATCH_MIN_BLOCKS4 : 32 / TY)
+__global__ void __launch_bounds__(32 * TY,
+                                  TY == 4 ? (NOISE ? 8 : EBSD_BATCH_MIN_BLOCKS4) : 32 / TY)
     k_forward_batched(const BatchJob* __restrict__ jobs,
                                                              const BatchHeader* __restrict__ hdr,
                                                              unsigned long long* __restrict__ counter)
