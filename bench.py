@@ -403,6 +403,7 @@ def run_ours(args):
             try:
                 if name == "c3":
                     legs["c3"] = c3_measure(args, 3)
+                    legs["c3"]["small_jobs"] = small_jobs_measure(args, 5)
                 elif name == "c4":
                     legs["c4"] = c4_measure(args, 5, 3)
                 elif name == "c5":
@@ -749,8 +750,103 @@ def c3_measure(args, steps: int) -> dict:
     return res
 
 
+def small_jobs_measure(args, steps: int, njobs: int = 256) -> dict:
+    """Many small jobs -- njobs (seed 5) of 1 to 32 orientations (log-uniform)
+    on 80x60 and 160x120 detectors of both phases, binning 1 or 2, gamma
+    0.33 -- where one launch per job is bound by launch latency and grid
+    tails: the batch (every job in the persistent queue, one CUDA graph)
+    against one launch per job, and against one launch per job captured in
+    a CUDA graph."""
+    import numpy as np
+    import torch
+
+    from ctemsoft_gb300 import capi, synth
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(5)
+    dets = {}
+    for ph in ("Ni", "Ti"):
+        wl = synth.c3_phase(ph)
+        sr, acc = wl.master(), wl.mc()
+        mh = capi.Handle(0)
+        mh.set_master(sr)
+        for nx, ny in ((80, 60), (160, 120)):
+            h = capi.Handle(0)
+            h.share_master(mh)
+            h.set_detector(dict(L=15000.0, thetac=10.0, delta=12800.0 / nx, numsx=nx, numsy=ny,
+                                xpc=0.0, ypc=0.0, sig=70.0), acc, 1, 11)
+            dets[(ph, nx)] = h
+        dets[(ph, "master")] = mh
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    jobs = []
+    for j in range(njobs):
+        ph = "Ni" if rng.random() < 0.5 else "Ti"
+        nx = 80 if rng.random() < 0.5 else 160
+        b = int(rng.choice([1, 2]))
+        n = int(np.clip(np.round(np.exp(rng.uniform(0.0, np.log(32.0)))), 1, 32))
+        src = dets[(ph, nx)]
+        h = capi.Handle(0)
+        h.share_detector(src)
+        h.set_stream(stream.cuda_stream)
+        epi = capi.epilogue(capi.prefactor(15.0, 100.0, src.num_el), binning=b,
+                            scalingmode="gam", gammavalue=0.33)
+        ox, oy = h.output_dims(epi)
+        q = torch.from_numpy(synth.shoemake_quaternions(n, 5000 + j)).to(dev)
+        jobs.append((h, q, epi, torch.empty((n, oy, ox), device=dev)))
+    total = sum(q.shape[0] for _, q, _, _ in jobs)
+    runner = capi.Handle(0)
+    runner.set_stream(stream.cuda_stream)
+
+    def one_by_one():
+        for h, q, epi, out in jobs:
+            h.forward(q, epi, out=out)
+
+    def timed(fn):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / steps
+
+    ms_b = timed(lambda: runner.forward_batched(jobs, graph=True))
+    ref = [out.clone() for *_, out in jobs]
+    ms_s = timed(one_by_one)
+    same = all(torch.equal(r, out) for r, (*_, out) in zip(ref, jobs))
+    # the per-job launches captured once in a CUDA graph and replayed
+    try:
+        graph = torch.cuda.CUDAGraph()
+        one_by_one()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=stream, capture_error_mode="thread_local"):
+            one_by_one()
+        ms_g = timed(graph.replay)
+        graphed = {"value": total / (ms_g / 1e3), "ms_per_step": ms_g}
+    except Exception as ex:
+        graphed = {"error": f"{type(ex).__name__}: {ex}"}
+    torch.cuda.set_stream(torch.cuda.default_stream(dev))
+    res = {"jobs": njobs, "patterns": total, "value": total / (ms_b / 1e3), "unit": UNIT,
+           "ms_per_step": ms_b,
+           "one_by_one": {"value": total / (ms_s / 1e3), "ms_per_step": ms_s},
+           "one_by_one_graph": graphed,
+           "identical": bool(same),
+           "what": "256 jobs of 1-32 orientations on 80x60/160x120: the persistent queue "
+                   "(one graph) against one launch per job, plain and graph-captured"}
+    for h, *_ in jobs:
+        h.close()
+    for h in list(dets.values()) + [runner]:
+        h.close()
+    return res
+
+
 def run_batched(args):
     res = c3_measure(args, args.steps)
+    res["small_jobs"] = small_jobs_measure(args, args.steps)
     line = dict(res, n_gpus=1, warmup=args.warmup, higher_is_better=True, dtype="f32",
                 data="synthetic",
                 config={"workload": f"batched-{res['patterns']}-patterns-seed2",

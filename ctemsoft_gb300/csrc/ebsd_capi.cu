@@ -50,10 +50,12 @@ struct DetectorTables {
     float4* W = nullptr;
     float4* drg = nullptr;
     float4* dW = nullptr;
+    double* rg64 = nullptr;  // [3][P] binary64 directions (binary64-geometry mode)
     int P = 0, NV = 0;
     ~DetectorTables()
     {
         cudaSetDevice(device);
+        cudaFree(rg64);
         cudaFree(rg);
         cudaFree(W);
         cudaFree(drg);
@@ -291,6 +293,11 @@ int fill_params(ebsd_handle* h, const ebsd_epilogue* e, FwdParams& p)
     p.scl = host::lambert_scale(h->npx);
     p.spi2 = host::lambert_spi2_f();
     p.accurate = h->lambert_accurate;
+    if (h->lambert_accurate == 2 && h->NV > 8)
+        return set_err(h, EBSD_EUNSUPPORTED,
+                       "lambert_accurate 2 (binary64 geometry): at most 32 energy bins");
+    p.rg64 = h->det ? h->det->rg64 : nullptr;
+    p.scl64 = (double)h->npx / 1.25331413731550025121;  // npx / sqrt(pi/2)
     p.o_offset = h->noise_offset;
     if (e) {
         if (e->scalingmode < EBSD_SCALING_NOT || e->scalingmode > EBSD_SCALING_GAM)
@@ -461,7 +468,9 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
             return set_err(h, EBSD_ESTATE, "l2_persist: no persisting window on this device/detector");
         }
     } else if (k == "lambert_accurate") {
-        h->lambert_accurate = value != 0;
+        if (value < 0 || value > 2)
+            return set_err(h, EBSD_EINVAL, "lambert_accurate must be 0, 1 or 2");
+        h->lambert_accurate = (int)value;
     } else if (k == "tile_y") {
         if (value != 4 && value != 8 && value != 16)
             return set_err(h, EBSD_EINVAL, "tile_y must be 4, 8 or 16");
@@ -605,6 +614,7 @@ int detector_setup(ebsd_handle* h, const ebsd_geometry* g, bool with_num_el)
         CK(h, cudaMalloc(&t->W, sizeof(float4) * (size_t)P * NV), "cudaMalloc W");
         CK(h, cudaMalloc(&t->drg, sizeof(float4) * (size_t)P * 3), "cudaMalloc drg");
         CK(h, cudaMalloc(&t->dW, sizeof(float4) * (size_t)P * (2 * NV + 1)), "cudaMalloc dW");
+        CK(h, cudaMalloc(&t->rg64, sizeof(double) * 3 * (size_t)P), "cudaMalloc rg64");
         t->P = P;
         t->NV = NV;
         h->det = std::move(t);
@@ -617,6 +627,7 @@ int detector_setup(ebsd_handle* h, const ebsd_geometry* g, bool with_num_el)
     float ca, sa;
     host::detector_angles(g->sig, g->thetac, &ca, &sa);
     CK(h, launch_detector(*g, ca, sa, h->d_rg, s), "detector kernel");
+    CK(h, launch_detector64(*g, h->det->rg64, s), "binary64 detector kernel");
     const float sclmc = host::lambert_scale(h->nsx);
     // kept by the handle: a refinement of the pattern centre sets the detector
     // up every iteration
@@ -1511,8 +1522,10 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         b.p.quats = (const float4*)J.quats;
         b.p.out = J.out;
         b.p.n = J.n;
-        if (!(flags & EBSD_BATCH_QUEUE_ALL) &&
-            forward_ctas(b.p, src->cfg) >= (int64_t)kBatchLargeCtasPerSm * sms) {
+        // the binary64-geometry mode exists only in the per-job pattern kernel
+        if (b.p.accurate == 2 ||
+            (!(flags & EBSD_BATCH_QUEUE_ALL) &&
+             forward_ctas(b.p, src->cfg) >= (int64_t)kBatchLargeCtasPerSm * sms)) {
             BatchLarge L;
             memset(&L, 0, sizeof L);
             L.p = b.p;
@@ -1842,6 +1855,9 @@ extern "C" int ebsd_forward_cells(ebsd_handle* h, const float* quats, int64_t n,
     if (n == 0) return EBSD_OK;
     if (e->poisson)
         return set_err(h, EBSD_EUNSUPPORTED, "ebsd_forward_cells: no noise in the cells variant");
+    if (h->lambert_accurate == 2)
+        return set_err(h, EBSD_EUNSUPPORTED,
+                       "ebsd_forward_cells: no cells variant of the binary64 geometry");
     if (ptr_kind(quats) != kDevice || ptr_kind(out) != kDevice || ptr_kind(nix) != kDevice ||
         ptr_kind(niy) != kDevice || ptr_kind(ixy0) != kDevice || ptr_kind(ixy1) != kDevice)
         return set_err(h, EBSD_EINVAL, "ebsd_forward_cells: every array must be device memory");
@@ -1867,6 +1883,8 @@ extern "C" int ebsd_cells(ebsd_handle* h, const float* quats, int64_t n, int32_t
     if (n == 0) return EBSD_OK;
     rc = check_device_home(h, "ebsd_cells", {quats, nix, niy, ixy0, ixy1});
     if (rc) return rc;
+    if (h->lambert_accurate == 2)
+        return set_err(h, EBSD_EUNSUPPORTED, "ebsd_cells: no cells variant of the binary64 geometry");
     rc = activate(h);
     if (rc) return rc;
     ebsd_epilogue unit;

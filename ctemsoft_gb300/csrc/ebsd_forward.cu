@@ -124,6 +124,59 @@ __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, fl
     ixy1 = scl * Y;
 }
 
+// Binary64 geometry of one pixel for one orientation: the FP64
+// re-evaluation of CTEMEBSD.f90:584-598 (the rotation, normalisation and fold
+// of :584-589, Lambert2DSquareInverseDouble of Lambert.f90:452-483, the cell
+// of :593-598) from the binary64 detector direction (rx, ry, rz); the
+// bilinear fractions are rounded once to binary32.  A single-precision
+// Lambert coordinate near |ixy| = npx = 500 resolves 3e-5 of a cell, which
+// on a sharp master moves a pixel by ~1e-4 of the pattern maximum; here the
+// coordinate carries binary64 accuracy.
+__device__ __forceinline__ void pixel_cell64(const float4 q, double rx, double ry, double rz,
+                                             double scl, int npx, int npy, int& ix0, int& iy0,
+                                             float& fdx, float& fdy)
+{
+    const double q0 = q.x, q1 = q.y, q2 = q.z, q3 = q.w;
+    const double y1 = -q1, y2 = -q2, y3 = -q3;                 // conjg(q)
+    const double t0 = -(rx * y1) - ry * y2 - rz * y3;          // (0, r) (x) conjg(q)
+    const double t1 = rx * q0 + ry * y3 - rz * y2;
+    const double t2 = -(rx * y3) + ry * q0 + rz * y1;
+    const double t3 = rx * y2 - ry * y1 + rz * q0;
+    double d0 = q0 * t1 + q1 * t0 + q2 * t3 - q3 * t2;         // q (x) t, vector part
+    double d1 = q0 * t2 - q1 * t3 + q2 * t0 + q3 * t1;
+    double d2 = q0 * t3 + q1 * t2 - q2 * t1 + q3 * t0;
+    const double n = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    d0 = d0 / n;
+    d1 = d1 / n;
+    d2 = d2 / n;
+    if (d2 < 0.0) {
+        d0 = -d0;
+        d1 = -d1;
+        d2 = -d2;
+    }
+    const double spi2 = 0.88622692545275801365;  // sqrt(pi)/2
+    double X = 0.0, Y = 0.0;
+    const double s2 = d0 * d0 + d1 * d1 + d2 * d2;
+    if (!(fabs(1.0 - s2) > 1.0e-12) && fabs(d2) != 1.0) {
+        if (fabs(d1) <= fabs(d0)) {
+            const double qq = copysign(sqrt(2.0 * (1.0 - d2)), d0);
+            X = qq * spi2;
+            Y = qq * atan(d1 / d0) / spi2;
+        } else {
+            const double qq = copysign(sqrt(2.0 * (1.0 - d2)), d1);
+            X = qq * atan(d0 / d1) / spi2;
+            Y = qq * spi2;
+        }
+    }
+    const double ixy0 = scl * X, ixy1 = scl * Y;
+    const int nix = (int)((double)npx + ixy0) - npx;
+    const int niy = (int)((double)npy + ixy1) - npy;
+    fdx = (float)(ixy0 - (double)nix);
+    fdy = (float)(ixy1 - (double)niy);
+    ix0 = min(max(nix + npx, 0), 2 * npx);
+    iy0 = min(max(niy + npy, 0), 2 * npy);
+}
+
 // One work item: the 32 x tile_y pixels of tile t for orientations
 // [o_begin, o_begin + opc).  `tile` is shared scratch of tile_y x 33 floats.
 // BIN8: the variant for 8x8-binned records outside the reference-order mode
@@ -132,8 +185,10 @@ __device__ __forceinline__ void pixel_lambert(const float4 q, const float4 r, fl
 // each pixel's Lambert cell and coordinates (prm.nix, niy, ixy0, ixy1, one
 // value per orientation and detector pixel) -- a diagnostic instantiation
 // of this template, so that cell parity is read out of the code that makes
-// the patterns.
-template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false>
+// the patterns.  G64: the pixel geometry in binary64 (pixel_cell64, option
+// lambert_accurate = 2).
+template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false,
+          bool G64 = false>
 __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, int tiles_x, int t,
                                              int64_t o_begin, int opc, float* tile, int bw)
 {
@@ -170,6 +225,12 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
     float4 w[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) w[c] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    double r64x = 0.0, r64y = 0.0, r64z = 1.0;
+    if (G64 && inside) {
+        r64x = prm.rg64[p];
+        r64y = prm.rg64[prm.P + p];
+        r64z = prm.rg64[2 * (int64_t)prm.P + p];
+    }
     if (inside) {
         r = ldg4_keep(prm.rg + p, pol);
 #pragma unroll
@@ -184,12 +245,17 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
         float val = 0.0f;
         if (inside) {
             const float4 q = ldg4(prm.quats + o);
-            float ixy0, ixy1;
-            pixel_lambert(q, r, prm.scl, prm.spi2, prm.accurate != 0, ixy0, ixy1);
             float dx, dy;
-            int nix, niy;
-            const int ix0 = lambert_cell(ixy0, prm.npx, dx, nix);
-            const int iy0 = lambert_cell(ixy1, prm.npy, dy, niy);
+            int ix0, iy0;
+            float ixy0 = 0.0f, ixy1 = 0.0f;
+            int nix = 0, niy = 0;
+            if (G64) {
+                pixel_cell64(q, r64x, r64y, r64z, prm.scl64, prm.npx, prm.npy, ix0, iy0, dx, dy);
+            } else {
+                pixel_lambert(q, r, prm.scl, prm.spi2, prm.accurate != 0, ixy0, ixy1);
+                ix0 = lambert_cell(ixy0, prm.npx, dx, nix);
+                iy0 = lambert_cell(ixy1, prm.npy, dy, niy);
+            }
             const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
             if (CELLS) {
                 const int64_t ci = o * (int64_t)prm.P + p;
@@ -303,15 +369,15 @@ int resolve_opc(int opc, int64_t n, int ntiles)
 #define EBSD_FWD_LAUNCH_BOUNDS __launch_bounds__(512)
 #endif
 
-template <int NV, bool STRICT, bool NOISE, bool BIN8, bool CELLS = false>
+template <int NV, bool STRICT, bool NOISE, bool BIN8, bool CELLS = false, bool G64 = false>
 __global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y, int tiles_x,
                                                  int ntiles, int opc, int warp_w)
 {
     extern __shared__ float tile[];  // [tile_y][33], binning only
     const int t = (int)(blockIdx.x % (unsigned)ntiles);
     const int64_t o_begin = (int64_t)(blockIdx.x / (unsigned)ntiles) * opc;
-    forward_tile<NV, STRICT, NOISE, BIN8, CELLS>(prm, tile_y, tiles_x, t, o_begin, opc, tile,
-                                                 warp_w);
+    forward_tile<NV, STRICT, NOISE, BIN8, CELLS, G64>(prm, tile_y, tiles_x, t, o_begin, opc, tile,
+                                                      warp_w);
 }
 
 // Batched pattern loop: one persistent grid works through a queue of work
@@ -394,7 +460,8 @@ __global__ void __launch_bounds__(32 * TY,
     }
 }
 
-template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false>
+template <int NV, bool STRICT, bool NOISE, bool BIN8 = false, bool CELLS = false,
+          bool G64 = false>
 cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
 {
     // binned records are summed inside a CTA: its height must hold whole
@@ -417,14 +484,26 @@ cudaError_t launch_nv2(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s)
     cudaLaunchAttribute attr[1];
     set_persist_attr(cfg, attr, lc);
     const int warp_w = cfg.warp_w == 32 ? 32 : 16;
-    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE, BIN8, CELLS>, p, tile_y, tiles_x,
-                              ntiles, opc, warp_w);
+    return cudaLaunchKernelEx(&lc, k_forward<NV, STRICT, NOISE, BIN8, CELLS, G64>, p, tile_y,
+                              tiles_x, ntiles, opc, warp_w);
 }
 
 template <int NV>
 cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s, bool cells)
 {
     const bool bin8 = !cfg.strict && p.mode != EBSD_SCALING_NOT && p.binning == 8;
+    if (p.accurate == 2) {  // binary64 geometry (fused gather; no cells variant; <= 32 bins)
+        if constexpr (NV <= 8) {
+            if (cells || !p.rg64) return cudaErrorInvalidValue;
+            const bool b8 = p.mode != EBSD_SCALING_NOT && p.binning == 8;
+            if (p.poisson)
+                return b8 ? launch_nv2<NV, false, true, true, false, true>(p, cfg, s)
+                          : launch_nv2<NV, false, true, false, false, true>(p, cfg, s);
+            return b8 ? launch_nv2<NV, false, false, true, false, true>(p, cfg, s)
+                      : launch_nv2<NV, false, false, false, false, true>(p, cfg, s);
+        }
+        return cudaErrorInvalidValue;
+    }
     if (cells)  // the diagnostic instantiations (no noise)
         return cfg.strict ? launch_nv2<NV, true, false, false, true>(p, cfg, s)
                : bin8     ? launch_nv2<NV, false, false, true, true>(p, cfg, s)

@@ -40,7 +40,9 @@ struct FwdParams {
     int poisson;
     uint64_t seed;
     int64_t o_offset;      // index of quats[0] within the call (noise streams)
-    int accurate;          // cancellation-free 1 - z near the poles
+    int accurate;          // 1: cancellation-free 1 - z near the poles; 2: binary64 geometry
+    const double* rg64;    // [3][P] binary64 directions (accurate == 2)
+    double scl64;          // npx / sqrt(pi/2) in binary64
     // diagnostics (the cells instantiation of the pattern kernel): [n][P]
     int32_t* nix;
     int32_t* niy;
@@ -112,6 +114,8 @@ cudaError_t launch_master_relayout(const float* raw, int npx, int npy, int nE, i
                                    int e0, int nsel, int NV, float4* il, cudaStream_t s);
 cudaError_t launch_detector(const ebsd_geometry& g, float ca, float sa, float4* rg,
                             cudaStream_t s);
+// binary64 directions, [3][P] (x, y, z planes)
+cudaError_t launch_detector64(const ebsd_geometry& g, double* rg64, cudaStream_t s);
 cudaError_t launch_weights(const float4* rg, int P, const int32_t* accum_e, int nE, int nsx,
                            int nsy, float sclmc, float spi2, int e0, int nsel, int NV, int fp64,
                            const ebsd_geometry& g, float4* W, float4* Wref, cudaStream_t s);

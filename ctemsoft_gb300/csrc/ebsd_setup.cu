@@ -221,6 +221,45 @@ cudaError_t launch_weights(const float4* rg, int P, const int32_t* accum_e, int 
     return cudaGetLastError();
 }
 
+// Detector direction cosines in binary64 (the FP64 re-evaluation of
+// CTEMEBSD.f90:416-452 that the binary64-geometry pattern kernel starts
+// from): three planes x, y, z of P doubles, pixel p = i + numsx*j.
+__global__ void k_detector64(WeightsGeom gd, double* __restrict__ rg64)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= gd.numsx || j >= gd.numsy) return;
+    const double sxp = -(gd.xpc - (1.0 - gd.numsx) * 0.5 - i) * gd.delta;
+    const double syp = (gd.ypc - (1.0 - gd.numsy) * 0.5 - j) * gd.delta;
+    const double Ls = gd.ca * syp + gd.L * gd.sa;
+    const double Lc = -gd.sa * syp + gd.L * gd.ca;
+    const double rh = 1.0 / sqrt(gd.L * gd.L + syp * syp + sxp * sxp);
+    const double x = Ls * rh, y = sxp * rh, z = Lc * rh;
+    const double n = sqrt(x * x + y * y + z * z);
+    const int64_t P = (int64_t)gd.numsx * gd.numsy, p = (int64_t)j * gd.numsx + i;
+    rg64[p] = x / n;
+    rg64[P + p] = y / n;
+    rg64[2 * P + p] = z / n;
+}
+
+cudaError_t launch_detector64(const ebsd_geometry& g, double* rg64, cudaStream_t s)
+{
+    WeightsGeom gd;
+    const double dtor = (double)0.0174533f;
+    const double alp = 0.5 * 3.141592653589793238 - ((double)(float)g.sig - (double)g.thetac) * dtor;
+    gd.L = g.L;
+    gd.delta = g.delta;
+    gd.xpc = g.xpc;
+    gd.ypc = g.ypc;
+    gd.ca = cos(alp);
+    gd.sa = sin(alp);
+    gd.numsx = g.numsx;
+    gd.numsy = g.numsy;
+    dim3 grid((g.numsx + 127) / 128, g.numsy);
+    k_detector64<<<grid, 128, 0, s>>>(gd, rg64);
+    return cudaGetLastError();
+}
+
 // num_el = nint(sum(accum_e_detector)), CTEMEBSD.f90:516.  gfortran sums
 // the array sequentially in single precision in memory order (bin fastest,
 // then x, then y); bins outside the window add exact zeros, and so do the

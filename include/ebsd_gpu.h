@@ -105,7 +105,17 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    multiply.
  *   "lambert_accurate" 0 (default): 1 - z as Lambert.f90:427,430 evaluate it;
  *                    1: (x^2 + y^2) / (1 + z), free of the cancellation near
- *                    the poles (cells may then differ from the reference's).
+ *                    the poles (cells may then differ from the reference's);
+ *                    2: the pattern kernel's per-pixel geometry (rotation,
+ *                    normalisation, Lambert map, cell and fractions) in
+ *                    binary64 from binary64 detector directions -- the
+ *                    FP64 re-evaluation of CTEMEBSD.f90:416-598 -- with the
+ *                    gather in binary32: within 1e-5 of FP64 pixel by pixel
+ *                    on 1001^2 masters, where a binary32 Lambert coordinate
+ *                    resolves only 3e-5 of a cell; several times slower
+ *                    (GB300's binary64 rate), at most 32 energy bins, no
+ *                    cells diagnostic, batched jobs run as their own
+ *                    launches.
  *   "l2_persist"     0 drops the persisting L2 window that ebsd_set_master
  *                    places on the master (kept by default where the device
  *                    offers one; 1 keeps it, an error if there is none).

@@ -23,6 +23,10 @@ import numpy as np
 #   coordinate near |ixy| = 500 resolves 3e-5 of a cell (one ulp), so a
 #   few ulps of binary32 geometry move a pixel on a sharp band edge by
 #   ~1e-4 of the pattern maximum whatever 1 - z is computed as.
+# * binary64 geometry (lambert_accurate = 2): the rotation, normalisation,
+#   Lambert map and cell of every pixel in binary64 from binary64 detector
+#   directions, the gather in binary32: within TOL_FP64 of FP64 pixel-wise
+#   on both masters.
 # * the default (binary64 weights, the reference's 1 - z): within TOL_FP64
 #   of FP64 as relative L2 and TOL_PIXEL_REF pixel-wise.  Single pixels near
 #   the Lambert poles differ from FP64 by up to ~1e-4 of the pattern maximum

@@ -118,6 +118,8 @@ def _three_modes(wl, q, n_f32=None):
     rep = cell_report(cells, det.cells(q, wl.npx), wl.npx, wl.npx)
     h.set_option("lambert_accurate", 1)
     acc_out = h.forward(q, epi)
+    h.set_option("lambert_accurate", 2)
+    g64_out = h.forward(q, epi)
     h.close()
     # reference arithmetic: single-precision weights, reference summation order
     hr, detr, _, num_el_r = _setup(wl, fp64=False)
@@ -128,8 +130,8 @@ def _three_modes(wl, q, n_f32=None):
     nt = O.max_threads()
     p64 = det.patterns_f64(sr, q, pref, nthreads=nt)
     p32 = det.patterns_f32(sr, q, pref, nthreads=nt)
-    return dict(default=out, accurate=acc_out, reference=ref_out, p64=p64, p32=p32, cells=rep,
-                pref=pref, det=det, sr=sr)
+    return dict(default=out, accurate=acc_out, binary64=g64_out, reference=ref_out, p64=p64,
+                p32=p32, cells=rep, pref=pref, det=det, sr=sr)
 
 
 def _gate_three_modes(tag, r, accurate_pixel=TOL_FP64):
@@ -148,6 +150,9 @@ def _gate_three_modes(tag, r, accurate_pixel=TOL_FP64):
     l2, mx = rel_errors(r["accurate"], r["p64"])
     print(tag, "accurate vs FP64: relL2 %.3g pixel %.3g" % (l2.max(), mx.max()))
     assert l2.max() <= TOL_FP64 and mx.max() <= accurate_pixel
+    l2, mx = rel_errors(r["binary64"], r["p64"])
+    print(tag, "binary64 geometry vs FP64: relL2 %.3g pixel %.3g" % (l2.max(), mx.max()))
+    assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64
 
 
 def test_c1_parity(built):
@@ -444,3 +449,37 @@ def test_shared_detector_matches_own_setup_and_copies_on_write(built):
     assert np.array_equal(s2.forward(q, epi), own)
     s.close()
     s2.close()
+
+
+def test_binary64_geometry_epilogues_batch_and_refusals(built):
+    """Option lambert_accurate = 2 (binary64 geometry): every epilogue
+    against the FP64 oracle pixel by pixel, a batched job equal to its own
+    launch, and the cells diagnostic refused."""
+    torch = pytest.importorskip("torch")
+    O = _oracle()
+    wl = synth.tiny(seed=5, numsx=64, numsy=48, npx=60, nE=5, mc_nsx=80, n_orient=9)
+    wl.delta = 60.0
+    wl.name = wl.name + "-b64"
+    h, det, sr, num_el = _setup(wl)
+    h.set_option("lambert_accurate", 2)
+    q = wl.quaternions()
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    p64 = det.patterns_f64(sr, q, pref)
+    for b, mode in ((1, "not"), (1, "gam"), (2, "lin"), (4, "gam"), (8, "lin"), (8, "gam")):
+        out = h.forward(q, capi.epilogue(pref, binning=b, scalingmode=mode, gammavalue=0.33))
+        ref = np.stack([O.epilogue_f64(p, b, capi.SCALING[mode], 0.33) for p in p64])
+        l2, mx = rel_errors(out, ref)
+        assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64, (b, mode, l2.max(), mx.max())
+    epi = capi.epilogue(pref, binning=2, scalingmode="gam", gammavalue=0.33)
+    dq = torch.from_numpy(q).cuda()
+    ox, oy = h.output_dims(epi)
+    out = torch.full((len(q), oy, ox), -1.0, device="cuda")
+    capi.Handle(0).forward_batched([(h, dq, epi, out)], graph=True, queue_all=True)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), h.forward(q, epi))
+    with pytest.raises(capi.EBSDError) as e:
+        h.cells(q)
+    assert e.value.code == capi.EBSD_EUNSUPPORTED
+    with pytest.raises(capi.EBSDError):
+        h.set_option("lambert_accurate", 3)
+    h.close()
