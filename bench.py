@@ -671,13 +671,15 @@ def c3_measure(args, steps: int) -> dict:
     setup_s = time.perf_counter() - t0
     t1 = time.perf_counter()
     jobs = []
+    shapes = {}  # tuned launch shapes (pixels x orientations per CTA) of the jobs
     for sp in specs:
         src = dets[(sp["numsx"], sp["numsy"], sp["delta"], sp["phase"])]
         h = capi.Handle(0)
         h.share_detector(src)
         epi = capi.epilogue(capi.prefactor(15.0, 100.0, src.num_el), binning=sp["binning"],
                             scalingmode="gam", gammavalue=0.33)
-        h.autotune(epi, 64, cache)
+        ty, oc, _ = h.autotune(epi, 64, cache)
+        shapes[f"32x{ty}x{oc}"] = shapes.get(f"32x{ty}x{oc}", 0) + 1
         ox, oy = h.output_dims(epi)
         q = torch.from_numpy(synth.shoemake_quaternions(sp["n"], sp["seed"])).to(dev)
         out = torch.empty((sp["n"], oy, ox), device=dev)
@@ -738,6 +740,7 @@ def c3_measure(args, steps: int) -> dict:
                             "what": "every job through the persistent queue kernel"},
         "identical_to_one_by_one": bool(same),
         "setup_s": setup_s, "autotune_s": tune_s, "first_batch_s": first_s,
+        "tuned_shapes": shapes,
         "e2e_with_setup": {"value": total / (setup_s + tune_s + first_s), "unit": UNIT,
                            "what": "detector set-up + launch-shape tuning (cached per shape "
                                    "in a file) + the first batch (graph capture and run)"},

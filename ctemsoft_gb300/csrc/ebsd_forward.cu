@@ -145,26 +145,30 @@ __device__ __forceinline__ void pixel_cell64(const float4 q, double rx, double r
     double d0 = q0 * t1 + q1 * t0 + q2 * t3 - q3 * t2;         // q (x) t, vector part
     double d1 = q0 * t2 - q1 * t3 + q2 * t0 + q3 * t1;
     double d2 = q0 * t3 + q1 * t2 - q2 * t1 + q3 * t0;
-    const double n = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-    d0 = d0 / n;
-    d1 = d1 / n;
-    d2 = d2 / n;
+    // binary64 divides and the arctangent run on GB300's slow binary64
+    // pipe: one reciprocal normalises (within an ulp of three divides), and
+    // 1/spi2 is a constant
+    const double in = 1.0 / sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    d0 = d0 * in;
+    d1 = d1 * in;
+    d2 = d2 * in;
     if (d2 < 0.0) {
         d0 = -d0;
         d1 = -d1;
         d2 = -d2;
     }
-    const double spi2 = 0.88622692545275801365;  // sqrt(pi)/2
+    const double spi2 = 0.88622692545275801365;   // sqrt(pi)/2
+    const double ispi2 = 1.12837916709551257390;  // 2/sqrt(pi)
     double X = 0.0, Y = 0.0;
     const double s2 = d0 * d0 + d1 * d1 + d2 * d2;
     if (!(fabs(1.0 - s2) > 1.0e-12) && fabs(d2) != 1.0) {
         if (fabs(d1) <= fabs(d0)) {
             const double qq = copysign(sqrt(2.0 * (1.0 - d2)), d0);
             X = qq * spi2;
-            Y = qq * atan(d1 / d0) / spi2;
+            Y = qq * atan(d1 / d0) * ispi2;
         } else {
             const double qq = copysign(sqrt(2.0 * (1.0 - d2)), d1);
-            X = qq * atan(d0 / d1) / spi2;
+            X = qq * atan(d0 / d1) * ispi2;
             Y = qq * spi2;
         }
     }

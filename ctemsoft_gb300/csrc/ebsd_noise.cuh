@@ -65,6 +65,13 @@ struct PixelRng {
           k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), call(0), used(4)
     {
     }
+    // Draw the next block now (the block the next call of next() would
+    // draw), so that code paths that diverge afterwards share its cost.
+    __device__ void fill()
+    {
+        blk = philox4x32_10(c0, c1, c2, call++, k0, k1);
+        used = 0;
+    }
     __device__ float next()
     {
         if (used == 4) {
@@ -125,9 +132,15 @@ __device__ __forceinline__ float log_poisson_pmf(float k, float lambda, float lo
 // hold up warps of PTRS draws.
 constexpr float kInversionMax = 10.0f;
 
-// One Poisson(lambda) draw.  lambda <= 0 (or NaN) gives 0.
+// One Poisson(lambda) draw.  lambda <= 0 (or NaN) gives 0.  rng is a fresh
+// stream (nothing drawn yet): both samplers start with its first block,
+// which is drawn here, before the lanes of a warp split between inversion
+// and PTRS, so a warp whose pixels straddle kInversionMax (most of them at
+// the reference's beam settings) runs the ten Philox rounds once, not once
+// per branch; the uniforms are the same.
 __device__ __forceinline__ float poisson_draw(float lambda, PixelRng& rng)
 {
+    rng.fill();
     if (!(lambda > 0.0f)) return 0.0f;
     if (lambda < kInversionMax) {
         // inversion: walk the cumulative distribution from k = 0.  Rounding
