@@ -66,9 +66,9 @@ def _args():
     ap.add_argument("--dict-steps", type=int, default=100,
                     help="dict: cubochoric steps per semi-edge of the m-3m zone")
     ap.add_argument("--fd-iters", type=int, default=3)
-    ap.add_argument("--legs", default="c3,c4,c5",
+    ap.add_argument("--legs", default="c3,c4,c5,program",
                     help="workloads added to the default line as sub-objects (comma list of "
-                         "c3, c4, c5; empty for none)")
+                         "c3, c4, c5, program; empty for none)")
     ap.add_argument("--legs-fd-iters", type=int, default=2,
                     help="c5 leg of the default line: finite-difference baseline iterations")
     return ap.parse_args()
@@ -406,6 +406,8 @@ def run_ours(args):
                     legs["c3"]["small_jobs"] = small_jobs_measure(args, 5)
                 elif name == "c4":
                     legs["c4"] = c4_measure(args, 5, 3)
+                elif name == "program":
+                    legs["program"] = program_measure(args)
                 elif name == "c5":
                     legs["c5"] = c5_measure(args, args.legs_fd_iters)
                     legs["c5"]["fd_note"] = (f"forward-only finite-difference baseline capped "
@@ -845,6 +847,64 @@ def small_jobs_measure(args, steps: int, njobs: int = 256) -> dict:
     for h in list(dets.values()) + [runner]:
         h.close()
     return res
+
+
+def program_measure(args, n: int = 20000, n_file: int = 4000) -> dict:
+    """The drop-in program end to end (ebsd_run_namelist, the reference's
+    CTEMEBSD with its namelist, angle, MC and master files): the 640x480
+    detector on the 1001^2 x 11 Ni master, gamma 0.33, with and without the
+    reference's Poisson noise; n orientations with the records written to
+    /dev/null (compute, device-to-host, record assembly), n_file written to
+    a file in the temporary directory (plus the page cache and file
+    system).  Wall time of the call,
+    file reading and detector set-up included, as the reference's program
+    would be timed from the shell."""
+    import shutil
+
+    from ctemsoft_gb300 import capi, formats, synth
+    wl = synth.C2
+    d = Path(tempfile.mkdtemp(prefix="ebsd_program_"))
+    try:
+        sr, acc = wl.master(), wl.mc()
+        formats.write_mc_file(d / "mc.data", acc, EkeV=wl.EkeV, Ehistmin=wl.Ehistmin,
+                              Ebinsize=wl.Ebinsize, sig=wl.sig)
+        formats.write_master_file(d / "master.data", sr, wl.energies)
+        for k, m in (("angles.txt", n), ("angles_file.txt", n_file)):
+            formats.write_angle_file(d / k, quats=synth.shoemake_quaternions(m, 1))
+        base = dict(L=wl.L, thetac=wl.thetac, delta=wl.delta, numsx=wl.numsx, numsy=wl.numsy,
+                    xpc=wl.xpc, ypc=wl.ypc, anglefile=str(d / "angles.txt"),
+                    eulerconvention="tsl", FZfile=str(d / "master.data"),
+                    energyfile=str(d / "mc.data"), beamcurrent=wl.beamcurrent,
+                    dwelltime=wl.dwelltime, energymin=10.0, energymax=20.0, binning=1,
+                    scalingmode="gam", gammavalue=wl.gammavalue)
+        res = {"orientations": {"devnull": n, "file": n_file},
+               "record_bytes": 4 * wl.numsx * wl.numsy,
+               "what": "ebsd_run_namelist wall time: namelist, angle/MC/master file reading, "
+                       "detector set-up, all patterns, records written"}
+        capi.run_namelist(_nml(d, base, "/dev/null", False), 0)  # warm-up (CUDA context, build)
+        for noise in (False, True):
+            for dest in ("/dev/null", str(d / "out.data")):
+                m = n if dest == "/dev/null" else n_file
+                cfg = dict(base, anglefile=str(d / ("angles.txt" if m == n else "angles_file.txt")))
+                t0 = time.perf_counter()
+                capi.run_namelist(_nml(d, cfg, dest, noise), 0)
+                dt = time.perf_counter() - t0
+                key = ("noise" if noise else "no_noise") + \
+                      ("_devnull" if dest == "/dev/null" else "_file")
+                res[key] = {"value": m / dt, "unit": UNIT, "wall_s": dt,
+                            "record_gbs": m * 4 * wl.numsx * wl.numsy / dt / 1e9}
+                if dest != "/dev/null":
+                    (d / "out.data").unlink()
+        return res
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+def _nml(d, base, dest, noise):
+    from ctemsoft_gb300 import formats
+    path = d / "run.nml"
+    formats.write_namelist(path, **dict(base, datafile=dest, poisson=noise, seed=3))
+    return path
 
 
 def run_batched(args):
