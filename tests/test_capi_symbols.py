@@ -64,6 +64,16 @@ def test_errors_without_side_effects(built):
         assert len(lib.ebsd_last_error(None)) > 0
     rc = lib.ebsd_create(C.byref(h), 10_000)
     assert rc in (capi.EBSD_ECUDA, capi.EBSD_EINVAL)
+    # the newer entry points refuse bad arguments before any CUDA call
+    assert lib.ebsd_share_detector(None, None) == capi.EBSD_EINVAL
+    assert lib.ebsd_forward_cells(None, None, 1, None, None, None, None, None, None) == \
+        capi.EBSD_EINVAL
+    assert lib.ebsd_run_namelist_devices(b"x.nml", None, 1, 1) == capi.EBSD_EINVAL
+    devs = (C.c_int32 * 1)(0)
+    assert lib.ebsd_run_namelist_devices(b"x.nml", devs, 0, 1) == capi.EBSD_EINVAL
+    assert lib.ebsd_run_namelist_devices(b"x.nml", devs, 65, 1) == capi.EBSD_EINVAL
+    assert lib.ebsd_refine_sharded(None, 1, None, None, None, None, None, None, None,
+                                   None) == capi.EBSD_EINVAL
     # the bandwidth probe checks its arguments before any CUDA call
     v = C.c_double()
     assert lib.ebsd_measure_bandwidth(0, 9, 1 << 20, 3, C.byref(v)) == capi.EBSD_EINVAL

@@ -172,3 +172,21 @@ def test_sharded_refinement_rejects_mixed_geometries(built):
     with pytest.raises(capi.EBSDError) as e:
         capi.refine_sharded([h, h2], [q[:4], q[4:]], epi, [targets[:4], targets[4:]])
     assert e.value.code == capi.EBSD_EINVAL and "geometry" in str(e.value)
+
+
+def test_sharded_refinement_with_an_empty_shard(built):
+    """A shard with no orientations takes no part in the accumulation but
+    still follows the shared pattern centre."""
+    torch = pytest.importorskip("torch")
+    wl, h, epi, qt, targets, true_geom = _problem(torch, 1, n=16, pc_shift=(0.3, -0.2, 5.0))
+    start = dict(h.geometry)
+    h2 = capi.Handle(0)
+    h2.share_master(h)
+    h2.set_detector(start, wl.mc(), 1, 5)
+    rng = np.random.default_rng(9)
+    q = torch.from_numpy(perturb(qt, 0.3, rng)).cuda()
+    empty = q[:0]
+    it, g = capi.refine_sharded([h, h2], [q, empty], epi, [targets, targets[:0]],
+                                max_iterations=6, refine_pc=True, damping=1e-4)
+    assert h2.geometry == g and h.geometry == g
+    assert abs(g["xpc"] - true_geom["xpc"]) < abs(start["xpc"] - true_geom["xpc"])

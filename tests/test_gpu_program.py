@@ -172,3 +172,18 @@ def test_resume_after_a_shard_stopped_early(built, tmp_path):
     _inputs(tmp_path, resume=True)
     capi.run_namelist(tmp_path / "run.nml", device=[0, 0])
     assert (tmp_path / "out.data").read_bytes() == full
+
+
+def test_device_list_errors(built, tmp_path):
+    """A device list naming a GPU that does not exist fails before any
+    output is written; sharing a detector from a handle without one is a
+    call-order error."""
+    _inputs(tmp_path)
+    with pytest.raises(capi.EBSDError) as e:
+        capi.run_namelist(tmp_path / "run.nml", device=[0, 999])
+    assert e.value.code in (capi.EBSD_EINVAL, capi.EBSD_ECUDA)
+    assert not (tmp_path / "out.data").exists()
+    a, b = capi.Handle(0), capi.Handle(0)
+    with pytest.raises(capi.EBSDError) as e:
+        b.share_detector(a)
+    assert e.value.code == capi.EBSD_ESTATE
