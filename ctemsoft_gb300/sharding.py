@@ -9,6 +9,11 @@ header record, then one (4*nx*ny + 8)-byte record per pattern).
 For Gauss-Newton refinement with one pattern centre shared by every
 pattern, each rank reduces its patterns to a 3x3 Schur-complement system of
 the centre; summing those 12 numbers across ranks is the only exchange.
+
+This module serves callers that run one process per GPU.  Within one
+process the C ABI does both without Python: ebsd_run_namelist_devices
+(one shard and host thread per device, records written at their offsets)
+and ebsd_refine_sharded (the 12 numbers summed in the process).
 """
 from __future__ import annotations
 
