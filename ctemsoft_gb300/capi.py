@@ -167,6 +167,8 @@ _SIGS = {
                               C.POINTER(C.c_int64)]),
     "ebsd_read_mc_namelist": (C.c_int, [C.c_char_p, C.POINTER(MCNamelist)]),
     "ebsd_run_mc_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
+    "ebsd_run_mc_namelist_devices": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.c_int32,
+                                               C.c_int]),
     "ebsd_run_namelist": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "ebsd_run_namelist_devices": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.c_int32,
                                             C.c_int]),
@@ -514,8 +516,15 @@ def run_namelist(path: str, device=0, quiet: bool = True) -> None:
         _check(lib().ebsd_run_namelist(str(path).encode(), device, int(quiet)))
 
 
-def run_mc_namelist(path: str, device: int = 0, quiet: bool = True) -> None:
-    _check(lib().ebsd_run_mc_namelist(str(path).encode(), device, int(quiet)))
+def run_mc_namelist(path: str, device=0, quiet: bool = True) -> None:
+    """The CTEMMC program for a namelist file; device is one index or a list
+    of indices (the electrons are split over them)."""
+    if isinstance(device, (list, tuple)):
+        arr = (C.c_int32 * len(device))(*device)
+        _check(lib().ebsd_run_mc_namelist_devices(str(path).encode(), arr, len(device),
+                                                  int(quiet)))
+    else:
+        _check(lib().ebsd_run_mc_namelist(str(path).encode(), device, int(quiet)))
 
 
 def read_mc_namelist(path: str) -> dict:

@@ -3,11 +3,13 @@
 // Same command line as the reference (files.f90:623-688): an optional
 // namelist file name (default CTEMMC.nml), -h for help and -t to write a
 // namelist template into the current folder; any flag stops the program
-// after it is handled.  One addition: -d N selects the CUDA device.
+// after it is handled.  One addition: -d N selects the CUDA device, and
+// -d N,M,... splits the electrons over several devices.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/ebsd_gpu.h"
 
@@ -54,7 +56,8 @@ void usage(const char* prog)
     printf(" If absent, the default name 'CTEMMC.nml' will be used.\n");
     printf(" To create a template of the input file, type %s -t\n", prog);
     printf(" To produce this message, type %s -h\n", prog);
-    printf(" -d N runs on CUDA device N (default 0).\n\n");
+    printf(" -d N runs on CUDA device N (default 0); -d N,M,... splits the electrons\n");
+    printf("    over several devices.\n\n");
 }
 
 }  // namespace
@@ -63,7 +66,7 @@ int main(int argc, char** argv)
 {
     std::string nml = "CTEMMC.nml";
     bool halt = false;
-    int device = 0;
+    std::vector<int32_t> devices;
     for (int i = 1; i < argc; ++i) {
         const char* a = argv[i];
         if (a[0] == '-') {
@@ -81,7 +84,17 @@ int main(int argc, char** argv)
                 printf("  -> created template file CTEMMC.template\n");
                 halt = true;
             } else if (!strcmp(a, "-d") && i + 1 < argc) {
-                device = atoi(argv[++i]);
+                devices.clear();
+                for (const char* q = argv[++i]; *q;) {
+                    char* end = nullptr;
+                    const long d = strtol(q, &end, 10);
+                    if (end == q || d < 0 || d > 1024 || (*end && *end != ',')) {
+                        fprintf(stderr, "bad device list %s\n", argv[i]);
+                        return 1;
+                    }
+                    devices.push_back((int32_t)d);
+                    q = *end == ',' ? end + 1 : end;
+                }
             } else {
                 fprintf(stderr, "unknown option %s\n", a);
                 halt = true;
@@ -94,7 +107,9 @@ int main(int argc, char** argv)
         printf("\nTo execute program, remove all flags except for nml input file name\n\n");
         return 0;
     }
-    const int rc = ebsd_run_mc_namelist(nml.c_str(), device, 0);
+    if (devices.empty()) devices.push_back(0);
+    const int rc =
+        ebsd_run_mc_namelist_devices(nml.c_str(), devices.data(), (int32_t)devices.size(), 0);
     if (rc != EBSD_OK) {
         fprintf(stderr, "CTEMMC: %s (code %d)\n", ebsd_last_error(nullptr), rc);
         return 1;

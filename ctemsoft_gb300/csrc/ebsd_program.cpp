@@ -448,9 +448,21 @@ extern "C" int ebsd_run_namelist_devices(const char* nmlfile, const int32_t* dev
 
 // The CTEMMC program on the GPU: CTEMMC.f90:48-277, the trajectory loop of
 // single_run replaced by ebsd_mc_run, the MC file written as the reference
-// writes it.
+// writes it.  On several GPUs each device runs a contiguous range of the
+// electrons into histograms of its own (every electron's random stream is
+// keyed by its index in the whole run), and the host adds them up: integer
+// sums, so the file is the one-device file byte for byte.
 extern "C" int ebsd_run_mc_namelist(const char* nmlfile, int device, int quiet)
 {
+    const int32_t d = device;
+    return ebsd_run_mc_namelist_devices(nmlfile, &d, 1, quiet);
+}
+
+extern "C" int ebsd_run_mc_namelist_devices(const char* nmlfile, const int32_t* devices,
+                                            int32_t ndev, int quiet)
+{
+    if (!devices || ndev < 1 || ndev > 64)
+        return fail(EBSD_EINVAL, "ebsd_run_mc_namelist_devices: 1 to 64 devices");
     auto say = [&](const char* fmt, auto... args) {
         if (!quiet) {
             printf(fmt, args...);
@@ -491,21 +503,51 @@ extern "C" int ebsd_run_mc_namelist(const char* nmlfile, int device, int quiet)
     rc = ebsd_mc_dims(&p, &nE, &nz);
     if (rc) return rc;
     const int nx = (nml.numsx - 1) / 2, n10 = nx / 10;
-    std::vector<int32_t> accum_e((size_t)nE * nml.numsx * nml.numsx);
-    std::vector<int32_t> accum_z((size_t)nE * nz * (2 * n10 + 1) * (2 * n10 + 1));
-    HandleGuard hg;
-    rc = ebsd_create(&hg.h, device);
-    if (rc) return rc;
+    const size_t ne = (size_t)nE * nml.numsx * nml.numsx;
+    const size_t nzs = (size_t)nE * nz * (2 * n10 + 1) * (2 * n10 + 1);
+    std::vector<int32_t> accum_e(ne);
+    std::vector<int32_t> accum_z(nzs);
+    std::vector<HandleGuard> hg(ndev);
+    for (int k = 0; k < ndev; ++k) {
+        rc = ebsd_create(&hg[k].h, devices[k]);
+        if (rc) return rc;
+    }
     const int64_t total = nml.num_el * (int64_t)nml.nthreads;
     say(" electrons: %lld x %d streams of the reference = %lld, one Philox stream each\n",
         (long long)nml.num_el, nml.nthreads, (long long)total);
     const auto t0 = std::chrono::steady_clock::now();
     int64_t counted = 0;
-    rc = ebsd_mc_run(hg.h, &p, (uint64_t)(uint32_t)nml.primeseed, 0, total, accum_e.data(),
-                     accum_z.data(), &counted);
-    if (rc) {
-        host::global_set_error(rc, ebsd_last_error(hg.h));
-        return rc;
+    {
+        // device k: electrons [total*k/ndev, total*(k+1)/ndev) into its own
+        // host histograms (device 0 straight into the result)
+        std::vector<std::vector<int32_t>> pe(ndev - 1), pz(ndev - 1);
+        std::vector<int64_t> cnt(ndev, 0);
+        std::vector<int> rcs(ndev, EBSD_OK);
+        std::vector<std::thread> th;
+        for (int k = 0; k < ndev; ++k) {
+            if (k > 0) {
+                pe[k - 1].assign(ne, 0);
+                pz[k - 1].assign(nzs, 0);
+            }
+            th.emplace_back([&, k] {
+                const int64_t a = total * k / ndev, b = total * (k + 1) / ndev;
+                int32_t* e = k ? pe[k - 1].data() : accum_e.data();
+                int32_t* z = k ? pz[k - 1].data() : accum_z.data();
+                rcs[k] = ebsd_mc_run(hg[k].h, &p, (uint64_t)(uint32_t)nml.primeseed, a, b - a, e,
+                                     z, &cnt[k]);
+            });
+        }
+        for (auto& t : th) t.join();
+        for (int k = 0; k < ndev; ++k)
+            if (rcs[k]) {
+                host::global_set_error(rcs[k], ebsd_last_error(hg[k].h));
+                return rcs[k];
+            }
+        for (int k = 0; k < ndev; ++k) counted += cnt[k];
+        for (int k = 1; k < ndev; ++k) {
+            for (size_t i = 0; i < ne; ++i) accum_e[i] += pe[k - 1][i];
+            for (size_t i = 0; i < nzs; ++i) accum_z[i] += pz[k - 1][i];
+        }
     }
     const double secs =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

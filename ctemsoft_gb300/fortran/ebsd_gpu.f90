@@ -147,6 +147,16 @@ module ebsd_gpu
       integer(c_int), value :: device, quiet
     end function
 
+    ! The CTEMMC program with the electrons split over several devices.
+    integer(c_int) function ebsd_run_mc_namelist_devices(nmlfile, devices, ndev, quiet) &
+        bind(C, name="ebsd_run_mc_namelist_devices")
+      import :: c_int, c_int32_t, c_char
+      character(kind=c_char), intent(in) :: nmlfile(*)  ! NUL-terminated
+      integer(c_int32_t), intent(in) :: devices(*)
+      integer(c_int32_t), value :: ndev
+      integer(c_int), value :: quiet
+    end function
+
     ! Tuning and precision options by name, e.g. "strict_order"//c_null_char.
     integer(c_int) function ebsd_set_option(h, key, val) bind(C, name="ebsd_set_option")
       import :: c_int, c_ptr, c_char, c_int64_t

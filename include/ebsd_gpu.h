@@ -457,6 +457,14 @@ int ebsd_read_mc_namelist(const char* path, ebsd_mc_namelist* nml);
  * reference's progress lines unless quiet != 0. */
 int ebsd_run_mc_namelist(const char* nmlfile, int device, int quiet);
 
+/* ebsd_run_mc_namelist on several GPUs: the electrons of CTEMMC.f90:307-529
+ * split into ndev contiguous ranges, one per listed device and host thread,
+ * each into histograms of its own, added up on the host; since every
+ * electron's stream is keyed by its index in the whole run, the MC file is
+ * byte for byte the single-device file.  ndev is 1..64. */
+int ebsd_run_mc_namelist_devices(const char* nmlfile, const int32_t* devices, int32_t ndev,
+                                 int quiet);
+
 /* ------------------------------------------------------------------ */
 /* File formats and the drop-in program                                 */
 /* ------------------------------------------------------------------ */

@@ -74,6 +74,7 @@ def test_errors_without_side_effects(built):
     assert lib.ebsd_run_namelist_devices(b"x.nml", devs, 65, 1) == capi.EBSD_EINVAL
     assert lib.ebsd_refine_sharded(None, 1, None, None, None, None, None, None, None,
                                    None) == capi.EBSD_EINVAL
+    assert lib.ebsd_run_mc_namelist_devices(b"x.nml", None, 1, 1) == capi.EBSD_EINVAL
     # the bandwidth probe checks its arguments before any CUDA call
     v = C.c_double()
     assert lib.ebsd_measure_bandwidth(0, 9, 1 << 20, 3, C.byref(v)) == capi.EBSD_EINVAL

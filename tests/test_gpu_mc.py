@@ -122,6 +122,31 @@ def test_ctemmc_program_feeds_the_pattern_loop(built, tmp_path, monkeypatch):
     assert np.isfinite(out).all() and out.max() > 0
 
 
+def test_ctemmc_device_list_writes_the_same_file(built, tmp_path, monkeypatch):
+    """The electrons split over a device list (the one GPU listed two and
+    three times: a handle and host thread each, histograms added on the
+    host) give the single-device MC file byte for byte; also through the
+    CLI's -d list."""
+    import subprocess
+    monkeypatch.chdir(tmp_path)
+    (tmp_path / "mc.nml").write_text(
+        "&MCdata xtalname = 'Ni.xtal', density = 8.908, Ze = 28.0, at_wt = 58.6934,\n"
+        " sig = 70.0, numsx = 121, num_el = 30001, nthreads = 3, primeseed = 7,\n"
+        " EkeV = 20.0, Ehistmin = 16.0, Ebinsize = 1.0, depthmax = 100.0, depthstep = 1.0,\n"
+        " dataname = 'MC.data' /\n")
+    capi.run_mc_namelist(tmp_path / "mc.nml", device=0)
+    one = (tmp_path / "MC.data").read_bytes()
+    for devs in ([0, 0], [0, 0, 0]):
+        (tmp_path / "MC.data").unlink()
+        capi.run_mc_namelist(tmp_path / "mc.nml", device=devs)
+        assert (tmp_path / "MC.data").read_bytes() == one, devs
+    (tmp_path / "MC.data").unlink()
+    exe = capi.LIB_PATH.parent / "ctemmc"
+    r = subprocess.run([str(exe), "-d", "0,0", "mc.nml"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "MC.data").read_bytes() == one
+
+
 def test_fp32_option_is_statistically_equivalent(built):
     """mc_fp32: the same trajectory steps in binary32.  On the same streams the
     two precisions start from the same draws and drift apart only by
