@@ -483,3 +483,29 @@ def test_binary64_geometry_epilogues_batch_and_refusals(built):
     with pytest.raises(capi.EBSDError):
         h.set_option("lambert_accurate", 3)
     h.close()
+
+
+@pytest.mark.parametrize("nE", [40, 64])
+def test_wide_energy_windows(built, nE):
+    """Energy windows of 40 and 64 bins (10 and 16 float4 per master node, the
+    widest the pattern kernel is built for) against the FP64 oracle, with a
+    window that leaves out the first and last bins (CTEMEBSD.f90:361-367)."""
+    O = _oracle()
+    wl = synth.tiny(seed=13, numsx=48, numsy=40, npx=40, nE=nE, mc_nsx=60, n_orient=5)
+    wl.name = f"{wl.name}-nE{nE}-wide"
+    Emin, Emax = 2, nE - 1
+    h, det, sr, num_el = _setup(wl, Emin=Emin, Emax=Emax, accurate=True)
+    assert num_el == det.num_el
+    q = wl.quaternions()
+    pref = capi.prefactor(wl.beamcurrent, wl.dwelltime, num_el)
+    for kw in (dict(), dict(binning=2, scalingmode="gam", gammavalue=0.4)):
+        out = h.forward(q, capi.epilogue(pref, **kw))
+        p64 = det.patterns_f64(sr, q, pref)
+        if kw:
+            p64 = np.stack([O.epilogue_f64(p, 2, 2, 0.4) for p in p64])
+        l2, mx = rel_errors(out, p64)
+        assert l2.max() <= TOL_FP64 and mx.max() <= TOL_FP64, (nE, kw, l2.max(), mx.max())
+    with pytest.raises(capi.EBSDError) as e:  # the adjoint serves windows of up to 32 bins
+        h.vjp(q, capi.epilogue(pref), np.ones((len(q), 40, 48), np.float32), "ndp")
+    assert e.value.code == capi.EBSD_EUNSUPPORTED
+    h.close()
