@@ -1466,7 +1466,8 @@ namespace {
 struct BatchGroup {
     int NV;
     bool noise;
-    int ty;  // tile height of the group's launch
+    int ty;     // tile height of the group's launch
+    bool bin8;  // 8x8-binned records
     std::vector<BatchJob> jobs;
 };
 
@@ -1534,7 +1535,15 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
             large.push_back(L);
             continue;
         }
-        const int ty = batch_tile_y(b.p.mode == EBSD_SCALING_NOT ? 1 : b.p.binning);
+        // the job's tuned tile height, raised until binned records hold whole
+        // blocks, as its own launch would run it
+        int ty = src->cfg.tile_y;
+        const bool binned = b.p.mode != EBSD_SCALING_NOT && b.p.binning > 1;
+        if (binned)
+            while (ty % b.p.binning != 0 && ty < 16) ty *= 2;
+        const bool bin8 = binned && b.p.binning == 8;
+        if (!batch_shape_ok(ty, bin8))
+            return set_err(h, EBSD_EINVAL, "job %d: tile height %d", j, ty);
         b.tiles_x = (b.p.numsx + kTileX - 1) / kTileX;
         b.ntiles = b.tiles_x * ((b.p.numsy + ty - 1) / ty);
         // items of 32 x ty pixels x opc orientations, >= 4096 pixel-patterns:
@@ -1545,10 +1554,10 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         b.items = (long long)b.ntiles * ((J.n + b.opc - 1) / b.opc);
         const bool noise = J.epilogue.poisson != 0;
         auto g = std::find_if(groups.begin(), groups.end(), [&](const BatchGroup& x) {
-            return x.NV == src->NV && x.noise == noise && x.ty == ty;
+            return x.NV == src->NV && x.noise == noise && x.ty == ty && x.bin8 == bin8;
         });
         if (g == groups.end()) {
-            groups.push_back({src->NV, noise, ty, {}});
+            groups.push_back({src->NV, noise, ty, bin8, {}});
             g = groups.end() - 1;
         }
         g->jobs.push_back(b);
@@ -1557,7 +1566,8 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
     std::sort(groups.begin(), groups.end(), [](const BatchGroup& a, const BatchGroup& b) {
         if (a.NV != b.NV) return a.NV < b.NV;
         if (a.noise != b.noise) return a.noise < b.noise;
-        return a.ty < b.ty;
+        if (a.ty != b.ty) return a.ty < b.ty;
+        return a.bin8 < b.bin8;
     });
 
     // table: [headers][counters][jobs of group 0][jobs of group 1]...
@@ -1573,7 +1583,7 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
     CK(h, cudaStreamSynchronize(h->stream), "batch");
     std::vector<int> key;
     for (auto& g : groups) {
-        key.push_back(g.NV * 32 + (g.noise ? 16 : 0) + g.ty);
+        key.push_back(g.NV * 128 + (g.noise ? 64 : 0) + (g.bin8 ? 32 : 0) + g.ty);
         key.push_back((int)g.jobs.size());
     }
     // a large job's parameters are baked into the graph's kernel node: the
@@ -1629,10 +1639,10 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         memcpy(ht + gi * sizeof(BatchHeader), &hd, sizeof hd);
         memcpy(ht + job_off + jo * sizeof(BatchJob), g.jobs.data(), g.jobs.size() * sizeof(BatchJob));
         jo += g.jobs.size();
-        const int gk = g.NV * 32 + (g.noise ? 16 : 0) + g.ty;
+        const int gk = g.NV * 128 + (g.noise ? 64 : 0) + (g.bin8 ? 32 : 0) + g.ty;
         auto it = h->batch_grid.find(gk);
         if (it == h->batch_grid.end())
-            it = h->batch_grid.emplace(gk, batched_grid(g.NV, g.noise, g.ty)).first;
+            it = h->batch_grid.emplace(gk, batched_grid(g.NV, g.noise, g.ty, g.bin8)).first;
         grids[gi] = it->second;
     }
     cudaStream_t s = h->stream;
@@ -1650,7 +1660,7 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
                 (const BatchJob*)(dt + job_off + j0 * sizeof(BatchJob)),
                 (const BatchHeader*)(dt + gi * sizeof(BatchHeader)),
                 (unsigned long long*)(dt + cnt_off) + gi, groups[gi].NV, groups[gi].noise,
-                groups[gi].ty, grids[gi], s);
+                groups[gi].ty, groups[gi].bin8, grids[gi], s);
             j0 += groups[gi].jobs.size();
         }
         return e;

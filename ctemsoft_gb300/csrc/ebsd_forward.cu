@@ -389,16 +389,18 @@ __global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y
 // detectors, binnings and masters.  Each CTA takes the next item with one
 // atomic increment and stops when the queue is exhausted -- no CTA waits
 // on another, so nothing can spin.  Jobs are ordered by item_begin.
-// TY is the tile height (CTA = 32 x TY threads); a group's jobs all use it.
-// Noise-free 32 x 4 CTAs are held to 56 registers, so that nine are resident
-// per SM as for the per-job pattern kernel (55 registers): with eight (64
-// registers) every job of the 64-job workload through the queue ran at
-// 268.1 k patterns/s, with nine at 272.1 k.  The noise variant keeps eight
-// (its sampler spills at 56 registers); 32 x 8 CTAs get 1024 threads per SM.
+// TY is the tile height (CTA = 32 x TY threads: 4, 8 or 16, the job's tuned
+// tile height); a group's jobs all use it, and BIN8 (the 8x8-binned
+// variant of forward_tile).  Noise-free 32 x 4 CTAs are held to 56
+// registers, so that nine are resident per SM as for the per-job pattern
+// kernel (55 registers): with eight (64 registers) every job of the 64-job
+// workload through the queue ran at 268.1 k patterns/s, with nine at
+// 272.1 k.  The noise variant keeps eight (its sampler spills at 56
+// registers); 32 x 8 and 32 x 16 CTAs get 1024 threads per SM.
 #ifndef EBSD_BATCH_MIN_BLOCKS4
 #define EBSD_BATCH_MIN_BLOCKS4 9
 #endif
-template <int NV, bool NOISE, int TY>
+template <int NV, bool NOISE, int TY, bool BIN8>
 __global__ void __launch_bounds__(32 * TY,
                                   TY == 4 ? (NOISE ? 8 : EBSD_BATCH_MIN_BLOCKS4) : 32 / TY)
     k_forward_batched(const BatchJob* __restrict__ jobs,
@@ -458,8 +460,7 @@ __global__ void __launch_bounds__(32 * TY,
         for (int i = threadIdx.x; i < (int)(sizeof(FwdParams) / 4); i += blockDim.x)
             dst[i] = src[i];
         __syncthreads();
-        // TY 8 groups hold the 8x8-binned jobs only
-        forward_tile<NV, false, NOISE, TY == 8>(sp, TY, J.tiles_x, t, o_begin, J.opc, tile, 16);
+        forward_tile<NV, false, NOISE, BIN8>(sp, TY, J.tiles_x, t, o_begin, J.opc, tile, 16);
         __syncthreads();
     }
 }
@@ -520,75 +521,98 @@ cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s, 
                 : launch_nv2<NV, false, false>(p, cfg, s);
 }
 
-template <int NV, bool NOISE, int TY>
+template <int NV, bool NOISE, int TY, bool BIN8>
 cudaError_t launch_batched3(const BatchJob* jobs, const BatchHeader* hdr,
                             unsigned long long* counter, int grid, cudaStream_t s)
 {
-    k_forward_batched<NV, NOISE, TY><<<grid, 32 * TY, 0, s>>>(jobs, hdr, counter);
+    k_forward_batched<NV, NOISE, TY, BIN8><<<grid, 32 * TY, 0, s>>>(jobs, hdr, counter);
     return cudaGetLastError();
+}
+
+// The group shapes: (TY, BIN8) in {(4, no), (8, no), (8, yes), (16, no), (16, yes)}.
+template <int NV, bool NOISE>
+cudaError_t launch_batched_nv2(const BatchJob* jobs, const BatchHeader* hdr,
+                               unsigned long long* counter, int grid, int ty, bool bin8,
+                               cudaStream_t s)
+{
+    if (ty == 4 && !bin8) return launch_batched3<NV, NOISE, 4, false>(jobs, hdr, counter, grid, s);
+    if (ty == 8)
+        return bin8 ? launch_batched3<NV, NOISE, 8, true>(jobs, hdr, counter, grid, s)
+                    : launch_batched3<NV, NOISE, 8, false>(jobs, hdr, counter, grid, s);
+    if (ty == 16)
+        return bin8 ? launch_batched3<NV, NOISE, 16, true>(jobs, hdr, counter, grid, s)
+                    : launch_batched3<NV, NOISE, 16, false>(jobs, hdr, counter, grid, s);
+    return cudaErrorInvalidValue;
 }
 
 template <int NV>
 cudaError_t launch_batched_nv(const BatchJob* jobs, const BatchHeader* hdr,
                               unsigned long long* counter, int grid, bool noise, int ty,
-                              cudaStream_t s)
+                              bool bin8, cudaStream_t s)
 {
-    if (ty == 4)
-        return noise ? launch_batched3<NV, true, 4>(jobs, hdr, counter, grid, s)
-                     : launch_batched3<NV, false, 4>(jobs, hdr, counter, grid, s);
-    return noise ? launch_batched3<NV, true, 8>(jobs, hdr, counter, grid, s)
-                 : launch_batched3<NV, false, 8>(jobs, hdr, counter, grid, s);
+    return noise ? launch_batched_nv2<NV, true>(jobs, hdr, counter, grid, ty, bin8, s)
+                 : launch_batched_nv2<NV, false>(jobs, hdr, counter, grid, ty, bin8, s);
 }
 
-template <int NV, bool NOISE, int TY>
+template <int NV, bool NOISE, int TY, bool BIN8>
 int batched_grid3()
 {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV, NOISE, TY>, 32 * TY,
-                                                  0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_forward_batched<NV, NOISE, TY, BIN8>,
+                                                  32 * TY, 0);
     return sms * (per > 0 ? per : 1);
 }
 
-template <int NV>
-int batched_grid_nv(bool noise, int ty)
+template <int NV, bool NOISE>
+int batched_grid_nv2(int ty, bool bin8)
 {
-    if (ty == 4) return noise ? batched_grid3<NV, true, 4>() : batched_grid3<NV, false, 4>();
-    return noise ? batched_grid3<NV, true, 8>() : batched_grid3<NV, false, 8>();
+    if (ty == 4 && !bin8) return batched_grid3<NV, NOISE, 4, false>();
+    if (ty == 8) return bin8 ? batched_grid3<NV, NOISE, 8, true>() : batched_grid3<NV, NOISE, 8, false>();
+    if (ty == 16)
+        return bin8 ? batched_grid3<NV, NOISE, 16, true>() : batched_grid3<NV, NOISE, 16, false>();
+    return 0;
+}
+
+template <int NV>
+int batched_grid_nv(bool noise, int ty, bool bin8)
+{
+    return noise ? batched_grid_nv2<NV, true>(ty, bin8) : batched_grid_nv2<NV, false>(ty, bin8);
 }
 
 }  // namespace
 
 cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
                                    unsigned long long* counter, int NV, bool noise, int ty,
-                                   int grid, cudaStream_t s)
+                                   bool bin8, int grid, cudaStream_t s)
 {
-    if (ty != 4 && ty != 8) return cudaErrorInvalidValue;
+    if (!batch_shape_ok(ty, bin8)) return cudaErrorInvalidValue;
     switch (NV) {
-        case 1: return launch_batched_nv<1>(jobs, hdr, counter, grid, noise, ty, s);
-        case 2: return launch_batched_nv<2>(jobs, hdr, counter, grid, noise, ty, s);
-        case 3: return launch_batched_nv<3>(jobs, hdr, counter, grid, noise, ty, s);
-        case 4: return launch_batched_nv<4>(jobs, hdr, counter, grid, noise, ty, s);
-        case 5: return launch_batched_nv<5>(jobs, hdr, counter, grid, noise, ty, s);
-        case 6: return launch_batched_nv<6>(jobs, hdr, counter, grid, noise, ty, s);
-        case 7: return launch_batched_nv<7>(jobs, hdr, counter, grid, noise, ty, s);
-        case 8: return launch_batched_nv<8>(jobs, hdr, counter, grid, noise, ty, s);
+        case 1: return launch_batched_nv<1>(jobs, hdr, counter, grid, noise, ty, bin8, s);
+        case 2: return launch_batched_nv<2>(jobs, hdr, counter, grid, noise, ty, bin8, s);
+        case 3: return launch_batched_nv<3>(jobs, hdr, counter, grid, noise, ty, bin8, s);
+        case 4: return launch_batched_nv<4>(jobs, hdr, counter, grid, noise, ty, bin8, s);
+        case 5: return launch_batched_nv<5>(jobs, hdr, counter, grid, noise, ty, bin8, s);
+        case 6: return launch_batched_nv<6>(jobs, hdr, counter, grid, noise, ty, bin8, s);
+        case 7: return launch_batched_nv<7>(jobs, hdr, counter, grid, noise, ty, bin8, s);
+        case 8: return launch_batched_nv<8>(jobs, hdr, counter, grid, noise, ty, bin8, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
-int batched_grid(int NV, bool noise, int ty)
+int batched_grid(int NV, bool noise, int ty, bool bin8)
 {
+    if (!batch_shape_ok(ty, bin8)) return 0;
     switch (NV) {
-        case 1: return batched_grid_nv<1>(noise, ty);
-        case 2: return batched_grid_nv<2>(noise, ty);
-        case 3: return batched_grid_nv<3>(noise, ty);
-        case 4: return batched_grid_nv<4>(noise, ty);
-        case 5: return batched_grid_nv<5>(noise, ty);
-        case 6: return batched_grid_nv<6>(noise, ty);
-        case 7: return batched_grid_nv<7>(noise, ty);
-        case 8: return batched_grid_nv<8>(noise, ty);
+        case 1: return batched_grid_nv<1>(noise, ty, bin8);
+        case 2: return batched_grid_nv<2>(noise, ty, bin8);
+        case 3: return batched_grid_nv<3>(noise, ty, bin8);
+        case 4: return batched_grid_nv<4>(noise, ty, bin8);
+        case 5: return batched_grid_nv<5>(noise, ty, bin8);
+        case 6: return batched_grid_nv<6>(noise, ty, bin8);
+        case 7: return batched_grid_nv<7>(noise, ty, bin8);
+        case 8: return batched_grid_nv<8>(noise, ty, bin8);
         default: return 0;
     }
 }

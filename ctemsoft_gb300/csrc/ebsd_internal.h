@@ -65,8 +65,13 @@ struct VjpParams {
 };
 
 // Batched pattern loop (ebsd_forward.cu): a table of jobs in device memory.
-// batched CTAs are 32 x 4 pixels for binning up to 4, 32 x 8 for binning 8
-inline int batch_tile_y(int binning) { return binning > 4 ? 8 : 4; }
+// A queued job runs at its handle's tile height (32 x 4, 8 or 16 pixels,
+// raised until binned records hold whole blocks); 8x8-binned jobs (BIN8)
+// take 8 or 16 rows.
+inline bool batch_shape_ok(int ty, bool bin8)
+{
+    return (ty == 4 && !bin8) || ty == 8 || ty == 16;
+}
 constexpr int kBatchMaxJobsSmem = 512;  // job starts cached in shared memory
 
 struct BatchJob {
@@ -154,8 +159,8 @@ cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cud
                            bool cells = false);
 cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
                                    unsigned long long* counter, int NV, bool noise, int ty,
-                                   int grid, cudaStream_t s);
-int batched_grid(int NV, bool noise, int ty);
+                                   bool bin8, int grid, cudaStream_t s);
+int batched_grid(int NV, bool noise, int ty, bool bin8);
 
 // Cubochoric fundamental-zone sampling (ebsd_so3.cu).  Constants of
 // Lambert.f90:246-280 in binary64.
