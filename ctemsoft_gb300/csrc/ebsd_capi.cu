@@ -289,7 +289,7 @@ int fill_params(ebsd_handle* h, const ebsd_epilogue* e, FwdParams& p)
     p.P = h->P;
     p.npx = h->npx;
     p.npy = h->npy;
-    p.gx = 2 * h->npx + 1;
+    p.gx = master_pitch(h->npx, h->NV);
     p.scl = host::lambert_scale(h->npx);
     p.spi2 = host::lambert_spi2_f();
     p.accurate = h->lambert_accurate;
@@ -516,7 +516,7 @@ extern "C" int ebsd_set_master(ebsd_handle* h, const float* sr, int32_t npx, int
         return set_err(h, EBSD_EUNSUPPORTED, "ebsd_set_master: nE=%d exceeds %d energy bins", nE,
                        4 * kMaxNV);
     // the pattern kernels address master nodes with 32-bit offsets
-    if ((double)(2 * npx + 1) * (double)(2 * npy + 1) * kMaxNV >= 2147483648.0)
+    if ((double)(2 * npx + 8) * (double)(2 * npy + 1) * kMaxNV >= 2147483648.0)
         return set_err(h, EBSD_EUNSUPPORTED,
                        "ebsd_set_master: a %dx%d grid exceeds the 2^31 float4 node offsets",
                        2 * npx + 1, 2 * npy + 1);
@@ -694,7 +694,7 @@ extern "C" int ebsd_set_detector(ebsd_handle* h, const ebsd_geometry* g, const i
         auto it = h->ms->layouts.find(key);
         if (it == h->ms->layouts.end()) {
             const size_t bytes =
-                sizeof(float4) * (size_t)(2 * h->npx + 1) * (2 * h->npy + 1) * NV;
+                sizeof(float4) * (size_t)master_pitch(h->npx, NV) * (2 * h->npy + 1) * NV;
             float4* il = nullptr;
             CK(h, cudaMalloc(&il, bytes), "cudaMalloc master layout");
             cudaError_t e2 = launch_master_relayout(h->ms->raw, h->npx, h->npy, h->nE, h->numset,

@@ -7,20 +7,23 @@
 namespace ebsd {
 
 // sr = sum(srtmp,4) (CTEMEBSD.f90:404) restricted to bins e0..e0+nsel-1 and
-// re-laid out energy-fastest: il[(y*gx + x)*NV*4 + k], zero padded to NV*4.
-// The Fortran source is srtmp(x, y, E, set), x fastest.
-__global__ void k_master_relayout(const float* __restrict__ raw, int gx, int gy, int nE,
-                                  int numset, int e0, int nsel, int NV, float* __restrict__ il)
+// re-laid out energy-fastest: il[(y*pitch + x)*NV*4 + k], zero padded to
+// NV*4 bins and to `pitch` nodes per row (master_pitch).  The Fortran source
+// is srtmp(x, y, E, set), x fastest.
+__global__ void k_master_relayout(const float* __restrict__ raw, int gx, int gy, int pitch,
+                                  int nE, int numset, int e0, int nsel, int NV,
+                                  float* __restrict__ il)
 {
-    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t nodes = (int64_t)gx * gy;
-    if (node >= nodes) return;
-    const int64_t plane = nodes;               // elements per energy bin
+    const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= (int64_t)pitch * gy) return;
+    const int y = (int)(slot / pitch), x = (int)(slot - (int64_t)y * pitch);
+    const int64_t plane = (int64_t)gx * gy;    // elements per energy bin
     const int64_t setstride = plane * nE;      // elements per atom set
-    float* dst = il + node * (int64_t)NV * 4;
+    const int64_t node = (int64_t)y * gx + x;
+    float* dst = il + slot * (int64_t)NV * 4;
     for (int k = 0; k < NV * 4; ++k) {
         float s = 0.0f;
-        if (k < nsel) {
+        if (k < nsel && x < gx) {
             const float* src = raw + (int64_t)(e0 + k) * plane + node;
             for (int st = 0; st < numset; ++st) s = s + src[st * setstride];
         }
@@ -31,11 +34,11 @@ __global__ void k_master_relayout(const float* __restrict__ raw, int gx, int gy,
 cudaError_t launch_master_relayout(const float* raw, int npx, int npy, int nE, int numset,
                                    int e0, int nsel, int NV, float4* il, cudaStream_t s)
 {
-    const int gx = 2 * npx + 1, gy = 2 * npy + 1;
-    const int64_t nodes = (int64_t)gx * gy;
+    const int gx = 2 * npx + 1, gy = 2 * npy + 1, pitch = master_pitch(npx, NV);
+    const int64_t slots = (int64_t)pitch * gy;
     const int bs = 256;
-    const unsigned blocks = (unsigned)((nodes + bs - 1) / bs);
-    k_master_relayout<<<blocks, bs, 0, s>>>(raw, gx, gy, nE, numset, e0, nsel, NV,
+    const unsigned blocks = (unsigned)((slots + bs - 1) / bs);
+    k_master_relayout<<<blocks, bs, 0, s>>>(raw, gx, gy, pitch, nE, numset, e0, nsel, NV,
                                              reinterpret_cast<float*>(il));
     return cudaGetLastError();
 }
