@@ -130,7 +130,7 @@ struct ebsd_handle {
     LaunchCfg cfg;
     int mc_fp32 = 0;     // Monte-Carlo trajectories in binary32
     int host_direct = 1; // kernel stores straight into pinned host outputs
-    int vjp_tile_y = 4;  // adjoint / Gauss-Newton CTA height (8 for binning 8)
+    int vjp_tile_y = 0;  // adjoint / Gauss-Newton tile height; 0: the defaults below
     int vjp_opc = 8;     // adjoint orientations per CTA
     int gn_opc = 32;     // Gauss-Newton orientations per CTA
     int weights_fp64 = 1;
@@ -484,8 +484,8 @@ extern "C" int ebsd_set_option(ebsd_handle* h, const char* key, int64_t value)
     } else if (k == "host_direct") {
         h->host_direct = value != 0;
     } else if (k == "vjp_tile_y") {
-        if (value != 4 && value != 8)
-            return set_err(h, EBSD_EINVAL, "vjp_tile_y must be 4 or 8");
+        if (value != 4 && value != 8 && value != 16 && value != 32)
+            return set_err(h, EBSD_EINVAL, "vjp_tile_y must be 4, 8, 16 or 32");
         h->vjp_tile_y = (int)value;
     } else if (k == "gn_orient_per_cta") {
         if (value < 1 || value > 64)
@@ -982,7 +982,10 @@ extern "C" int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebs
     vp.dW = h->d_dW;
     vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
     vp.opc = h->vjp_opc;
-    const int tile_y = vp.binning > h->vjp_tile_y ? 8 : h->vjp_tile_y;
+    // unbinned records: 32 x 16 tiles by default (tile_y / 4 pixels per
+    // thread); binned ones a CTA of 32 x tile_y threads, at most 8 rows
+    int tile_y = h->vjp_tile_y > 0 ? h->vjp_tile_y : (vp.binning == 1 ? 16 : 4);
+    if (vp.binning > 1) tile_y = vp.binning > std::min(tile_y, 8) ? 8 : std::min(tile_y, 8);
     if (vp.binning > tile_y)
         return set_err(h, EBSD_EUNSUPPORTED, "ebsd_vjp: binning %d exceeds the tile", vp.binning);
     const int K = mode == EBSD_VJP_NDP ? 15 : 6;
@@ -1217,7 +1220,9 @@ extern "C" int ebsd_gn_accumulate(ebsd_handle* h, const float* quats, int64_t n,
     vp.dW = h->d_dW;
     vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
     vp.opc = h->gn_opc;
-    const int tile_y = vp.binning > h->vjp_tile_y ? 8 : h->vjp_tile_y;
+    // the Gauss-Newton kernel's CTA is 32 x tile_y threads (at most 8 rows)
+    const int ty_opt = h->vjp_tile_y > 0 ? std::min(h->vjp_tile_y, 8) : 4;
+    const int tile_y = vp.binning > ty_opt ? 8 : ty_opt;
     if (vp.binning > tile_y)
         return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: binning %d exceeds the tile",
                        vp.binning);

@@ -32,6 +32,49 @@ __device__ __forceinline__ float4 ldg4_keep(const float4* p, uint64_t pol)
     return v;
 }
 
+// Two binary32 values in one 64-bit register pair (low half first), for the
+// packed FP32 instructions of sm_100 and later (PTX fma/mul/add .rn.f32x2):
+// each half is one IEEE binary32 operation rounded to nearest, exactly the
+// scalar operation's result, two per issued instruction.  The sums below
+// that use them carry bins of even and odd index in the two halves.
+typedef unsigned long long f2_t;
+
+__device__ __forceinline__ f2_t f2_pack(float lo, float hi)
+{
+    f2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+
+__device__ __forceinline__ float f2_sum(f2_t v)  // lo + hi
+{
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    return lo + hi;
+}
+
+__device__ __forceinline__ f2_t f2_fma(f2_t a, f2_t b, f2_t c)
+{
+    f2_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b)
+{
+    f2_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// 128-bit read-only load with the L2 policy, as two pairs (x, y), (z, w).
+__device__ __forceinline__ void ldg4_keep2(const float4* p, uint64_t pol, f2_t& lo, f2_t& hi)
+{
+    asm("ld.global.nc.L2::cache_hint.v2.b64 {%0, %1}, [%2], %3;"
+        : "=l"(lo), "=l"(hi)
+        : "l"(p), "l"(pol));
+}
+
 // qq3 = q (x) (0,r) (x) conjg(q), quaternions.f90:255-264,306-313 as used at
 // CTEMEBSD.f90:577-586; returns the vector part.  The first product's terms
 // with the zero scalar part of (0,r) are left out: 0*y is +-0 for finite y,

@@ -71,17 +71,24 @@ __device__ __forceinline__ float gather_pixel(const float4* __restrict__ master,
         }
         return acc;
     }
-    float c00 = 0.0f, c10 = 0.0f, c01 = 0.0f, c11 = 0.0f;
+    // the four dot products on packed pairs of bins (even bins in the low
+    // halves, odd in the high), two fused multiply-adds per instruction
+    f2_t c00 = 0, c10 = 0, c01 = 0, c11 = 0;  // +0.0f pairs
 #pragma unroll
     for (int c = 0; c < NV; ++c) {
-        const float4 a = ldg4_keep(m00 + c, pol), b = ldg4_keep(m10 + c, pol),
-                     e = ldg4_keep(m01 + c, pol), f = ldg4_keep(m11 + c, pol);
-        c00 = fmaf(w[c].x, a.x, fmaf(w[c].y, a.y, fmaf(w[c].z, a.z, fmaf(w[c].w, a.w, c00))));
-        c10 = fmaf(w[c].x, b.x, fmaf(w[c].y, b.y, fmaf(w[c].z, b.z, fmaf(w[c].w, b.w, c10))));
-        c01 = fmaf(w[c].x, e.x, fmaf(w[c].y, e.y, fmaf(w[c].z, e.z, fmaf(w[c].w, e.w, c01))));
-        c11 = fmaf(w[c].x, f.x, fmaf(w[c].y, f.y, fmaf(w[c].z, f.z, fmaf(w[c].w, f.w, c11))));
+        f2_t a0, a1, b0, b1, e0, e1, f0, f1;
+        ldg4_keep2(m00 + c, pol, a0, a1);
+        ldg4_keep2(m10 + c, pol, b0, b1);
+        ldg4_keep2(m01 + c, pol, e0, e1);
+        ldg4_keep2(m11 + c, pol, f0, f1);
+        const f2_t w0 = f2_pack(w[c].x, w[c].y), w1 = f2_pack(w[c].z, w[c].w);
+        c00 = f2_fma(w1, a1, f2_fma(w0, a0, c00));
+        c10 = f2_fma(w1, b1, f2_fma(w0, b0, c10));
+        c01 = f2_fma(w1, e1, f2_fma(w0, e0, c01));
+        c11 = f2_fma(w1, f1, f2_fma(w0, f0, c11));
     }
-    return fmaf(c00, dxm * dym, fmaf(c10, dx * dym, fmaf(c01, dxm * dy, c11 * (dx * dy))));
+    return fmaf(f2_sum(c00), dxm * dym,
+                fmaf(f2_sum(c10), dx * dym, fmaf(f2_sum(c01), dxm * dy, f2_sum(c11) * (dx * dy))));
 }
 
 // Sum of the B x B binning block (B = 2 or 4) held by a warp of 32/B x B

@@ -109,7 +109,11 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     // slopes with four FMAs per bin; the weight derivatives need the
     // per-bin bilinear value bv.
     const float w00 = dxm * dym, w10 = dx * dym, w01 = dxm * dy, w11 = dx * dy;
-    float SA = 0.0f, SB = 0.0f, SC = 0.0f, SD = 0.0f, U0 = 0.0f, U1 = 0.0f;
+    // The sums run on packed pairs of bins (even bins in the low halves,
+    // odd in the high), two fused multiply-adds per instruction.
+    const f2_t W00 = f2_pack(w00, w00), W10 = f2_pack(w10, w10), W01 = f2_pack(w01, w01),
+               W11 = f2_pack(w11, w11);
+    f2_t pA = 0, pB = 0, pC = 0, pD = 0, pU0 = 0, pU1 = 0;  // +0.0f pairs
     // one float4 group of bins at a time: unrolling would hoist all
     // 8*NV vector loads and spill
     // dW_k/dtheta_a = G0_k di0_a + G1_k di1_a, so the weight terms need only
@@ -119,24 +123,27 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
     const int64_t plane = prm.P, eplane = (int64_t)NV * prm.P;
 #pragma unroll 1
     for (int c = 0; c < NV; ++c, wp += plane, ep += plane) {
-        const float4 A = ldg4_keep(m00 + c, pol), B = ldg4_keep(m10 + c, pol),
-                     C = ldg4_keep(m01 + c, pol), D = ldg4_keep(m11 + c, pol);
-        const float4 wc = ldg4_keep(wp, pol);
-        const float4 e0 = ldg4_keep(ep, pol);
-        const float4 e1 = ldg4_keep(ep + eplane, pol);
-#define EBSD_BIN(f)                                                                        \
-{                                                                                      \
-    const float bv = fmaf(A.f, w00, fmaf(B.f, w10, fmaf(C.f, w01, D.f * w11)));         \
-    SA = fmaf(wc.f, A.f, SA);                                                           \
-    SB = fmaf(wc.f, B.f, SB);                                                           \
-    SC = fmaf(wc.f, C.f, SC);                                                           \
-    SD = fmaf(wc.f, D.f, SD);                                                           \
-    U0 = fmaf(e0.f, bv, U0);                                                            \
-    U1 = fmaf(e1.f, bv, U1);                                                            \
-}
-        EBSD_BIN(x) EBSD_BIN(y) EBSD_BIN(z) EBSD_BIN(w)
-#undef EBSD_BIN
+        f2_t A[2], B[2], C[2], D[2], wc[2], e0[2], e1[2];
+        ldg4_keep2(m00 + c, pol, A[0], A[1]);
+        ldg4_keep2(m10 + c, pol, B[0], B[1]);
+        ldg4_keep2(m01 + c, pol, C[0], C[1]);
+        ldg4_keep2(m11 + c, pol, D[0], D[1]);
+        ldg4_keep2(wp, pol, wc[0], wc[1]);
+        ldg4_keep2(ep, pol, e0[0], e0[1]);
+        ldg4_keep2(ep + eplane, pol, e1[0], e1[1]);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const f2_t bv = f2_fma(A[h], W00, f2_fma(B[h], W10, f2_fma(C[h], W01, f2_mul(D[h], W11))));
+            pA = f2_fma(wc[h], A[h], pA);
+            pB = f2_fma(wc[h], B[h], pB);
+            pC = f2_fma(wc[h], C[h], pC);
+            pD = f2_fma(wc[h], D[h], pD);
+            pU0 = f2_fma(e0[h], bv, pU0);
+            pU1 = f2_fma(e1[h], bv, pU1);
+        }
     }
+    const float SA = f2_sum(pA), SB = f2_sum(pB), SC = f2_sum(pC), SD = f2_sum(pD);
+    const float U0 = f2_sum(pU0), U1 = f2_sum(pU1);
     const float P = fmaf(SA, w00, fmaf(SB, w10, fmaf(SC, w01, SD * w11)));
     const float gX = fmaf(SB - SA, dym, (SD - SC) * dy);
     const float gY = fmaf(SC - SA, dxm, (SD - SB) * dx);
@@ -268,6 +275,77 @@ __global__ void __launch_bounds__(256, EBSD_VJP_MIN_BLOCKS)
         const int ol = i / K, k = i - ol * K;
         float s2 = 0.0f;
         for (int wy = 0; wy < tile_y; ++wy) s2 += red[(ol * tile_y + wy) * K + k];
+        vp.partial[((o_begin + ol) * ntiles + t) * K + k] = s2;
+    }
+}
+
+// The adjoint for unbinned records: CTAs of four warps over a 32 x 4 PPT
+// pixel tile, each thread PPT pixels (rows ty, ty + 4, ...) of the tile.  A
+// thread adds its pixels' terms before the warp reduction, so the
+// reduction (about 85 instructions per warp-orientation) is paid once per
+// PPT pixels.  Each warp covers a 16 x 2 block of every 32 x 4 layer of
+// the tile in 4 x 2 quarter-warps, so that the 8 lanes whose 128-bit loads
+// the L1 serves together gather from a compact patch of the master.
+// Resident CTAs per SM for its register budget (a build-time knob): 5 (96
+// registers) measured 4-5 % faster at 640x480 and 480x480 than 6 (80,
+// where the loss mode spills at four pixels per thread) and 12 % faster
+// than 8 (64).
+#ifndef EBSD_VJP1_MIN_BLOCKS
+#define EBSD_VJP1_MIN_BLOCKS 5
+#endif
+template <int NV, int MODE, int PPT>
+__global__ void __launch_bounds__(128, EBSD_VJP1_MIN_BLOCKS)
+    k_vjp1(const FwdParams prm, const VjpParams vp, int tiles_x, int ntiles, int opc)
+{
+    constexpr int K = MODE == EBSD_VJP_NDP ? 15 : 6;
+    constexpr int KP = MODE == EBSD_VJP_NDP ? 16 : 8;
+    extern __shared__ float red[];  // [opc][4 warps][K] warp sums
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int tx = (wid & 1) * 16 + (lane >> 3) * 4 + (lane & 3);
+    const int ty = (wid >> 1) * 2 + ((lane >> 2) & 1);
+    // orientation blocks fastest across the grid (as k_vjp)
+    const unsigned n_ob = (unsigned)((prm.n + opc - 1) / opc);
+    const int t = (int)(blockIdx.x / n_ob);
+    const int64_t o_begin = (int64_t)(blockIdx.x % n_ob) * opc;
+    const int x = (t % tiles_x) * kTileX + tx;
+    const int y0 = (t / tiles_x) * (4 * PPT) + ty;
+    const uint64_t pol = l2_policy_evict_last();
+    const float pref = (float)prm.prefactor;
+    const int64_t rec = (int64_t)prm.P;  // unbinned: out_nx x out_ny = numsx x numsy
+
+    for (int64_t o = o_begin; o < o_begin + opc && o < prm.n; ++o) {
+        float acc[KP];
+#pragma unroll
+        for (int a = 0; a < KP; ++a) acc[a] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+            const int y = y0 + 4 * k;
+            if (x < prm.numsx && y < prm.numsy) {
+                const int p = y * prm.numsx + x;
+                float val, J[6];
+                pixel_value_jacobian<NV>(prm, vp, p, o, pol, pref, val, J);
+                const float dv = vp.data[o * rec + p];
+#pragma unroll
+                for (int a = 0; a < 6; ++a) acc[a] = fmaf(dv, J[a], acc[a]);
+                if (MODE == EBSD_VJP_NDP) {
+#pragma unroll
+                    for (int a = 0; a < 6; ++a) acc[6 + a] = fmaf(val, J[a], acc[6 + a]);
+                    acc[12] = fmaf(val, val, acc[12]);
+                    acc[13] = fmaf(val, dv, acc[13]);
+                    acc[14] = fmaf(dv, dv, acc[14]);
+                }
+            }
+        }
+        warp_reduce_scatter<KP>(acc, lane);
+        const int idx = lane / (32 / KP);
+        if (lane % (32 / KP) == 0 && idx < K) red[((o - o_begin) * 4 + wid) * K + idx] = acc[0];
+    }
+    __syncthreads();
+    const int no = (int)min((int64_t)opc, prm.n - o_begin);
+    for (int i = tid; i < no * K; i += blockDim.x) {
+        const int ol = i / K, k = i - ol * K;
+        float s2 = 0.0f;
+        for (int w = 0; w < 4; ++w) s2 += red[(ol * 4 + w) * K + k];
         vp.partial[((o_begin + ol) * ntiles + t) * K + k] = s2;
     }
 }
@@ -634,6 +712,26 @@ cudaError_t launch_vjp_nv(const FwdParams& p, const VjpParams& vp, int mode, int
     const int64_t blocks = ((p.n + opc - 1) / opc) * ntiles;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
     const int K = mode == EBSD_VJP_NDP ? 15 : 6;
+    if (vp.binning == 1 && tile_y % 4 == 0 && tile_y <= 32) {
+        // unbinned: four warps, tile_y / 4 pixels per thread
+        const size_t smem1 = sizeof(float) * (size_t)K * 4 * opc;
+        auto go1 = [&](auto kern) {
+            const cudaError_t e = allow_smem(kern, smem1);
+            if (e != cudaSuccess) return e;
+            kern<<<(unsigned)blocks, 128, smem1, s>>>(p, vp, tiles_x, ntiles, opc);
+            return cudaGetLastError();
+        };
+        const int ppt = tile_y / 4;
+        if (mode == EBSD_VJP_NDP)
+            return ppt == 1   ? go1(k_vjp1<NV, EBSD_VJP_NDP, 1>)
+                   : ppt == 2 ? go1(k_vjp1<NV, EBSD_VJP_NDP, 2>)
+                   : ppt == 4 ? go1(k_vjp1<NV, EBSD_VJP_NDP, 4>)
+                              : go1(k_vjp1<NV, EBSD_VJP_NDP, 8>);
+        return ppt == 1   ? go1(k_vjp1<NV, EBSD_VJP_COTANGENT, 1>)
+               : ppt == 2 ? go1(k_vjp1<NV, EBSD_VJP_COTANGENT, 2>)
+               : ppt == 4 ? go1(k_vjp1<NV, EBSD_VJP_COTANGENT, 4>)
+                          : go1(k_vjp1<NV, EBSD_VJP_COTANGENT, 8>);
+    }
     const size_t smem = sizeof(float) * (33 * tile_y + (size_t)K * tile_y * opc);
     const bool bsh = vp.binning == 2 || vp.binning == 4;
     auto go = [&](auto kern) {

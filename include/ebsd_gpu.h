@@ -124,8 +124,12 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *   "orient_per_cta" orientations per CTA, 1..64, or 0 (default): 64,
  *                    halved while the launch would have fewer than 32 CTAs
  *                    per SM.
- *   "vjp_tile_y"     CTA height of ebsd_vjp and the Gauss-Newton kernels:
- *                    4 (default) or 8; binning 8 always uses 8.
+ *   "vjp_tile_y"     tile height in pixels of ebsd_vjp and the Gauss-Newton
+ *                    kernels: 4, 8, 16 or 32.  Unbinned adjoint records: 16 by
+ *                    default (CTAs of 128 threads, tile_y / 4 pixels per
+ *                    thread).  Binned records and Gauss-Newton: 4 by
+ *                    default, at most 8 (one thread per pixel); binning 8
+ *                    always uses 8.
  *   "noise_index_offset"  the pattern index of the first orientation of the
  *                    next calls (default 0): Poisson noise is keyed by (seed,
  *                    pattern index, pixel), so a caller that computes a long
