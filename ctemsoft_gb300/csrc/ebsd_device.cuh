@@ -197,13 +197,24 @@ __device__ __forceinline__ void lambert_inverse_jac(float x, float y, float z, f
 // Cell index and bilinear fractions, CTEMEBSD.f90:593-598:
 // nix = int(npx + ixy) - npx (float add, then truncation), dx = ixy - nix.
 // Returns the 0-based grid column of the lower corner, clamped to the grid.
+//
+// The truncation is taken without the float/integer conversion instructions
+// (which run on a slower pipe): t = npx + ixy is the reference's binary32
+// sum; for 0 <= t < 2^23, adding 2^23 rounded toward zero leaves 2^23 +
+// int(t) exactly, whose low mantissa bits are int(t), and subtracting 2^23
+// again gives int(t) as an exact float, so dx = ixy - (int(t) - npx) is the
+// reference's value bit for bit.  t lies in that range: |ixy| <= npx up to a
+// few ulps (|X|, |Y| <= sqrt(pi/2) for unit directions, and the intercepted
+// ones map to 0), so t > -1, where int() gives 0 as max(t, 0) does.
+// (+0.8 % at 640x480 against cvt.rzi / cvt.rn.)
 __device__ __forceinline__ int lambert_cell(float ixy, int np, float& d, int& ni)
 {
-    ni = __float2int_rz((float)np + ixy) - np;
-    d = ixy - (float)ni;
-    int i0 = ni + np;
-    i0 = i0 < 0 ? 0 : (i0 > 2 * np ? 2 * np : i0);
-    return i0;
+    const float t = (float)np + ixy;
+    const float tt = __fadd_rz(fmaxf(t, 0.0f), 8388608.0f);  // 2^23 + int(t)
+    const int it = __float_as_int(tt) - 0x4B000000;          // int(t)
+    ni = it - np;
+    d = ixy - ((tt - 8388608.0f) - (float)np);
+    return min(it, 2 * np);
 }
 
 }  // namespace ebsd

@@ -252,6 +252,9 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
 
     int64_t o_end = o_begin + opc;
     if (o_end > prm.n) o_end = prm.n;
+    // two orientations per loop trip: the geometry of one overlaps the other's
+    // gather (640x480: +0.5 %; four per trip take 56 registers, -15 %)
+#pragma unroll 2
     for (int64_t o = o_begin; o < o_end; ++o) {
         float val = 0.0f;
         if (inside) {
