@@ -138,9 +138,7 @@ struct ebsd_handle {
     int64_t noise_offset = 0;  // pattern index of a call's first orientation (noise streams)
 
     // batched pattern loop: device job table, pinned host mirror, graph
-    DeviceBuf batch_table;
-    void* batch_table_host = nullptr;
-    size_t batch_table_host_bytes = 0;
+    DeviceBuf batch_table;     // the queue counters of the batch's launches
     cudaGraphExec_t batch_exec = nullptr;
     std::vector<int> batch_key;
     cudaStream_t batch_stream = nullptr;
@@ -428,7 +426,6 @@ extern "C" void ebsd_destroy(ebsd_handle* h)
     cudaFree(h->rfz.ptr);
     cudaFree(h->rfz_out.ptr);
     cudaFree(h->mc.ptr);
-    if (h->batch_table_host) cudaFreeHost(h->batch_table_host);
     if (h->batch_exec) cudaGraphExecDestroy(h->batch_exec);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
@@ -1575,24 +1572,49 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
         return a.bin8 < b.bin8;
     });
 
-    // table: [headers][counters][jobs of group 0][jobs of group 1]...
-    const size_t G = groups.size();
-    size_t njob_total = 0;
-    for (auto& g : groups) njob_total += g.jobs.size();
-    const size_t hdr_bytes = G * sizeof(BatchHeader);
-    const size_t cnt_off = (hdr_bytes + 255) & ~size_t(255);
-    const size_t job_off = (cnt_off + G * sizeof(unsigned long long) + 255) & ~size_t(255);
-    const size_t bytes = job_off + njob_total * sizeof(BatchJob);
-
-    // the previous batch must have consumed the pinned table before it is rewritten
-    CK(h, cudaStreamSynchronize(h->stream), "batch");
-    std::vector<int> key;
-    for (auto& g : groups) {
-        key.push_back(g.NV * 128 + (g.noise ? 64 : 0) + (g.bin8 ? 32 : 0) + g.ty);
-        key.push_back((int)g.jobs.size());
+    // launches of the queue kernel: each group's jobs in chunks of at most
+    // kBatchLaunchJobs, each chunk a launch with its own queue counter and
+    // its jobs in the kernel parameters
+    struct QueueLaunch {
+        size_t group;
+        std::unique_ptr<BatchLaunch> table;
+        int grid;
+    };
+    std::vector<QueueLaunch> qls;
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        auto& g = groups[gi];
+        const int gk = g.NV * 128 + (g.noise ? 64 : 0) + (g.bin8 ? 32 : 0) + g.ty;
+        auto it = h->batch_grid.find(gk);
+        if (it == h->batch_grid.end())
+            it = h->batch_grid.emplace(gk, batched_grid(g.NV, g.noise, g.ty, g.bin8)).first;
+        for (size_t j0 = 0; j0 < g.jobs.size(); j0 += kBatchLaunchJobs) {
+            const size_t nj = std::min(g.jobs.size() - j0, (size_t)kBatchLaunchJobs);
+            auto L = std::make_unique<BatchLaunch>();
+            memset(L.get(), 0, sizeof(BatchLaunch));
+            long long begin = 0;
+            for (size_t j = 0; j < nj; ++j) {
+                L->job[j] = g.jobs[j0 + j];
+                L->job[j].item_begin = begin;
+                begin += L->job[j].items;
+            }
+            L->total_items = begin;
+            L->njobs = (int)nj;
+            qls.push_back({gi, std::move(L), it->second});
+        }
     }
-    // a large job's parameters are baked into the graph's kernel node: the
-    // graph is reused only for identical parameters (the same buffers)
+    const size_t NQ = qls.size();
+
+    // (the counters are reset in stream order, so an earlier batch still in
+    // flight on this stream is not disturbed)
+    // a graph bakes every launch's parameters into its kernel nodes: it is
+    // reused only for an identical job list (the same buffers and sizes)
+    std::vector<int> key;
+    for (auto& q : qls) {
+        const auto& g = groups[q.group];
+        key.push_back(g.NV * 128 + (g.noise ? 64 : 0) + (g.bin8 ? 32 : 0) + g.ty);
+        const int* w = reinterpret_cast<const int*>(q.table.get());  // zero-filled padding
+        key.insert(key.end(), w, w + (16 + q.table->njobs * sizeof(BatchJob)) / sizeof(int));
+    }
     for (auto& L : large) {
         key.push_back(-1);
         const int* w = reinterpret_cast<const int*>(&L.p);  // zero-filled padding
@@ -1606,67 +1628,29 @@ extern "C" int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_
     }
     const bool use_graph = (flags & EBSD_BATCH_GRAPH) != 0;
     const bool reuse = use_graph && h->batch_exec && h->batch_key == key &&
-                       h->batch_table_host_bytes >= bytes && h->batch_stream == h->stream;
+                       h->batch_stream == h->stream;
     if (!reuse) {
         if (h->batch_exec) {
             cudaGraphExecDestroy(h->batch_exec);
             h->batch_exec = nullptr;
         }
     }
-    if (!reuse && G > 0) {
-        rc = ensure(h, h->batch_table, bytes, "batch table");
+    if (NQ > 0) {
+        rc = ensure(h, h->batch_table, NQ * sizeof(unsigned long long), "batch queue counters");
         if (rc) return rc;
-        if (h->batch_table_host_bytes < bytes) {
-            if (h->batch_table_host) cudaFreeHost(h->batch_table_host);
-            h->batch_table_host = nullptr;
-            h->batch_table_host_bytes = 0;
-            CK(h, cudaMallocHost(&h->batch_table_host, bytes), "pinned batch table");
-            h->batch_table_host_bytes = bytes;
-        }
     }
-    // fill the pinned table
-    char* ht = (char*)h->batch_table_host;
-    char* dt = (char*)h->batch_table.ptr;
-    if (G > 0) memset(ht, 0, bytes);
-    size_t jo = 0;
-    std::vector<int> grids(G);
-    for (size_t gi = 0; gi < G; ++gi) {
-        auto& g = groups[gi];
-        long long begin = 0;
-        for (auto& b : g.jobs) {
-            b.item_begin = begin;
-            begin += b.items;
-        }
-        BatchHeader hd;
-        memset(&hd, 0, sizeof hd);
-        hd.total_items = begin;
-        hd.njobs = (int)g.jobs.size();
-        memcpy(ht + gi * sizeof(BatchHeader), &hd, sizeof hd);
-        memcpy(ht + job_off + jo * sizeof(BatchJob), g.jobs.data(), g.jobs.size() * sizeof(BatchJob));
-        jo += g.jobs.size();
-        const int gk = g.NV * 128 + (g.noise ? 64 : 0) + (g.bin8 ? 32 : 0) + g.ty;
-        auto it = h->batch_grid.find(gk);
-        if (it == h->batch_grid.end())
-            it = h->batch_grid.emplace(gk, batched_grid(g.NV, g.noise, g.ty, g.bin8)).first;
-        grids[gi] = it->second;
-    }
+    unsigned long long* counters = (unsigned long long*)h->batch_table.ptr;
     cudaStream_t s = h->stream;
     auto enqueue = [&]() -> cudaError_t {
         cudaError_t e = cudaSuccess;
         for (size_t i = 0; i < large.size() && e == cudaSuccess; ++i)
             e = launch_forward(large[i].p, large[i].NV, large[i].cfg, s);
-        if (G == 0) return e;
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dt, ht, bytes, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess)
-            e = cudaMemsetAsync(dt + cnt_off, 0, G * sizeof(unsigned long long), s);
-        size_t j0 = 0;
-        for (size_t gi = 0; gi < G && e == cudaSuccess; ++gi) {
-            e = launch_forward_batched(
-                (const BatchJob*)(dt + job_off + j0 * sizeof(BatchJob)),
-                (const BatchHeader*)(dt + gi * sizeof(BatchHeader)),
-                (unsigned long long*)(dt + cnt_off) + gi, groups[gi].NV, groups[gi].noise,
-                groups[gi].ty, groups[gi].bin8, grids[gi], s);
-            j0 += groups[gi].jobs.size();
+        if (NQ == 0) return e;
+        if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, NQ * sizeof(unsigned long long), s);
+        for (size_t i = 0; i < NQ && e == cudaSuccess; ++i) {
+            const auto& g = groups[qls[i].group];
+            e = launch_forward_batched(*qls[i].table, counters + i, g.NV, g.noise, g.ty, g.bin8,
+                                       qls[i].grid, s);
         }
         return e;
     };

@@ -253,8 +253,11 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
     int64_t o_end = o_begin + opc;
     if (o_end > prm.n) o_end = prm.n;
     // two orientations per loop trip: the geometry of one overlaps the other's
-    // gather (640x480: +0.5 %; four per trip take 56 registers, -15 %)
-#pragma unroll 2
+    // gather (640x480: +0.5 %; four per trip take 56 registers, -15 %).  Not
+    // for the noise variant (100 registers instead of 64 at two: -29 %) nor
+    // the binary64-geometry and cells variants.
+    constexpr int kUnroll = (NOISE || G64 || CELLS) ? 1 : 2;
+#pragma unroll kUnroll
     for (int64_t o = o_begin; o < o_end; ++o) {
         float val = 0.0f;
         if (inside) {
@@ -399,35 +402,38 @@ __global__ void EBSD_FWD_LAUNCH_BOUNDS k_forward(const FwdParams prm, int tile_y
 // detectors, binnings and masters.  Each CTA takes the next item with one
 // atomic increment and stops when the queue is exhausted -- no CTA waits
 // on another, so nothing can spin.  Jobs are ordered by item_begin.
+// The jobs' parameters are kernel parameters (a __grid_constant__ table in
+// the constant bank): the pattern loop reads them through the constant
+// cache as the per-job kernel does, not from shared memory, which shares
+// the L1 data pipe with the master gathers (parameters staged in shared
+// memory cost about ten shared loads per warp and orientation).
 // TY is the tile height (CTA = 32 x TY threads: 4, 8 or 16, the job's tuned
 // tile height); a group's jobs all use it, and BIN8 (the 8x8-binned
-// variant of forward_tile).  Noise-free 32 x 4 CTAs are held to 56
-// registers, so that nine are resident per SM as for the per-job pattern
-// kernel (55 registers): with eight (64 registers) every job of the 64-job
-// workload through the queue ran at 268.1 k patterns/s, with nine at
-// 272.1 k.  The noise variant keeps eight (its sampler spills at 56
-// registers); 32 x 8 and 32 x 16 CTAs get 1024 threads per SM.
+// variant of forward_tile).  CTAs get 64 registers (1024 threads per SM):
+// the parameters read in the loop need registers of their own.  Every job
+// of the 64-job workload through the queue, patterns/s: 282.0 k at 64
+// registers, 280.5 k with nine 32 x 4 CTAs per SM (56), 273.0 k with ten 32 x
+// 4 and five 32 x 8 (48, spilling); with the parameters staged in shared
+// memory instead, 272.3 k (56 / 64 registers) and 276.2 k (48).
 #ifndef EBSD_BATCH_MIN_BLOCKS4
-#define EBSD_BATCH_MIN_BLOCKS4 9
+#define EBSD_BATCH_MIN_BLOCKS4 8
+#endif
+#ifndef EBSD_BATCH_MIN_BLOCKS8
+#define EBSD_BATCH_MIN_BLOCKS8 4
 #endif
 template <int NV, bool NOISE, int TY, bool BIN8>
 __global__ void __launch_bounds__(32 * TY,
-                                  TY == 4 ? (NOISE ? 8 : EBSD_BATCH_MIN_BLOCKS4) : 32 / TY)
-    k_forward_batched(const BatchJob* __restrict__ jobs,
-                                                             const BatchHeader* __restrict__ hdr,
-                                                             unsigned long long* __restrict__ counter)
+                                  TY == 4 ? (NOISE ? 8 : EBSD_BATCH_MIN_BLOCKS4)
+                                  : TY == 8 ? (NOISE ? 4 : EBSD_BATCH_MIN_BLOCKS8)
+                                            : 32 / TY)
+    k_forward_batched(const __grid_constant__ BatchLaunch L,
+                      unsigned long long* __restrict__ counter)
 {
     __shared__ float tile[TY * 33];
-    __shared__ long long s_begin[kBatchMaxJobsSmem];  // item_begin of each job
     __shared__ long long s_obegin[2];
-    __shared__ FwdParams sp;
     __shared__ int s_job[2], s_tile[2];
-    const int njobs = hdr->njobs;
-    const long long total = hdr->total_items;
-    const bool cached = njobs <= kBatchMaxJobsSmem;
-    if (cached)
-        for (int j = threadIdx.x; j < njobs; j += blockDim.x) s_begin[j] = jobs[j].item_begin;
-    __syncthreads();
+    const int njobs = L.njobs;
+    const long long total = L.total_items;
     // Thread 0 claims and decodes items one ahead: while the CTA computes
     // item k, the claim, the job search and the (64-bit) tile/orientation
     // split of item k+1 are already done by one thread instead of all.
@@ -440,13 +446,12 @@ __global__ void __launch_bounds__(32 * TY,
         int lo = 0, hi = njobs - 1;  // last job with item_begin <= it
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            const long long b = cached ? s_begin[mid] : jobs[mid].item_begin;
-            if (b <= it)
+            if (L.job[mid].item_begin <= it)
                 lo = mid;
             else
                 hi = mid - 1;
         }
-        const BatchJob& J = jobs[lo];
+        const BatchJob& J = L.job[lo];
         const long long local = it - J.item_begin;
         const long long ob = local / J.ntiles;
         s_job[slot] = lo;
@@ -455,22 +460,18 @@ __global__ void __launch_bounds__(32 * TY,
     };
     if (threadIdx.x == 0) claim(0);
     __syncthreads();
+    // One barrier per item: the next item's slot is written by thread 0
+    // while the others read this one's, and the barrier at the end of the
+    // item publishes it (it also keeps the CTA's warps on one item, whose
+    // gathers share L1 lines).
     for (int slot = 0;; slot ^= 1) {
         const int job = s_job[slot];
         if (job < 0) break;
         const int t = s_tile[slot];
         const int64_t o_begin = s_obegin[slot];
         if (threadIdx.x == 0) claim(slot ^ 1);
-        const BatchJob& J = jobs[job];
-        // the item's job parameters, staged in shared memory (read there as
-        // uniform operands; 1.7 % faster than reading them from the table)
-        static_assert(sizeof(FwdParams) % 4 == 0, "parameters copied as 32-bit words");
-        const int* src = reinterpret_cast<const int*>(&J.p);
-        int* dst = reinterpret_cast<int*>(&sp);
-        for (int i = threadIdx.x; i < (int)(sizeof(FwdParams) / 4); i += blockDim.x)
-            dst[i] = src[i];
-        __syncthreads();
-        forward_tile<NV, false, NOISE, BIN8>(sp, TY, J.tiles_x, t, o_begin, J.opc, tile, 16);
+        const BatchJob& J = L.job[job];
+        forward_tile<NV, false, NOISE, BIN8>(J.p, TY, J.tiles_x, t, o_begin, J.opc, tile, 16);
         __syncthreads();
     }
 }
@@ -532,36 +533,34 @@ cudaError_t launch_nv(const FwdParams& p, const LaunchCfg& cfg, cudaStream_t s, 
 }
 
 template <int NV, bool NOISE, int TY, bool BIN8>
-cudaError_t launch_batched3(const BatchJob* jobs, const BatchHeader* hdr,
-                            unsigned long long* counter, int grid, cudaStream_t s)
+cudaError_t launch_batched3(const BatchLaunch& L, unsigned long long* counter, int grid,
+                            cudaStream_t s)
 {
-    k_forward_batched<NV, NOISE, TY, BIN8><<<grid, 32 * TY, 0, s>>>(jobs, hdr, counter);
+    k_forward_batched<NV, NOISE, TY, BIN8><<<grid, 32 * TY, 0, s>>>(L, counter);
     return cudaGetLastError();
 }
 
 // The group shapes: (TY, BIN8) in {(4, no), (8, no), (8, yes), (16, no), (16, yes)}.
 template <int NV, bool NOISE>
-cudaError_t launch_batched_nv2(const BatchJob* jobs, const BatchHeader* hdr,
-                               unsigned long long* counter, int grid, int ty, bool bin8,
-                               cudaStream_t s)
+cudaError_t launch_batched_nv2(const BatchLaunch& L, unsigned long long* counter, int grid,
+                               int ty, bool bin8, cudaStream_t s)
 {
-    if (ty == 4 && !bin8) return launch_batched3<NV, NOISE, 4, false>(jobs, hdr, counter, grid, s);
+    if (ty == 4 && !bin8) return launch_batched3<NV, NOISE, 4, false>(L, counter, grid, s);
     if (ty == 8)
-        return bin8 ? launch_batched3<NV, NOISE, 8, true>(jobs, hdr, counter, grid, s)
-                    : launch_batched3<NV, NOISE, 8, false>(jobs, hdr, counter, grid, s);
+        return bin8 ? launch_batched3<NV, NOISE, 8, true>(L, counter, grid, s)
+                    : launch_batched3<NV, NOISE, 8, false>(L, counter, grid, s);
     if (ty == 16)
-        return bin8 ? launch_batched3<NV, NOISE, 16, true>(jobs, hdr, counter, grid, s)
-                    : launch_batched3<NV, NOISE, 16, false>(jobs, hdr, counter, grid, s);
+        return bin8 ? launch_batched3<NV, NOISE, 16, true>(L, counter, grid, s)
+                    : launch_batched3<NV, NOISE, 16, false>(L, counter, grid, s);
     return cudaErrorInvalidValue;
 }
 
 template <int NV>
-cudaError_t launch_batched_nv(const BatchJob* jobs, const BatchHeader* hdr,
-                              unsigned long long* counter, int grid, bool noise, int ty,
-                              bool bin8, cudaStream_t s)
+cudaError_t launch_batched_nv(const BatchLaunch& L, unsigned long long* counter, int grid,
+                              bool noise, int ty, bool bin8, cudaStream_t s)
 {
-    return noise ? launch_batched_nv2<NV, true>(jobs, hdr, counter, grid, ty, bin8, s)
-                 : launch_batched_nv2<NV, false>(jobs, hdr, counter, grid, ty, bin8, s);
+    return noise ? launch_batched_nv2<NV, true>(L, counter, grid, ty, bin8, s)
+                 : launch_batched_nv2<NV, false>(L, counter, grid, ty, bin8, s);
 }
 
 template <int NV, bool NOISE, int TY, bool BIN8>
@@ -593,20 +592,20 @@ int batched_grid_nv(bool noise, int ty, bool bin8)
 
 }  // namespace
 
-cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
-                                   unsigned long long* counter, int NV, bool noise, int ty,
-                                   bool bin8, int grid, cudaStream_t s)
+cudaError_t launch_forward_batched(const BatchLaunch& L, unsigned long long* counter, int NV,
+                                   bool noise, int ty, bool bin8, int grid, cudaStream_t s)
 {
-    if (!batch_shape_ok(ty, bin8)) return cudaErrorInvalidValue;
+    if (!batch_shape_ok(ty, bin8) || L.njobs < 1 || L.njobs > kBatchLaunchJobs)
+        return cudaErrorInvalidValue;
     switch (NV) {
-        case 1: return launch_batched_nv<1>(jobs, hdr, counter, grid, noise, ty, bin8, s);
-        case 2: return launch_batched_nv<2>(jobs, hdr, counter, grid, noise, ty, bin8, s);
-        case 3: return launch_batched_nv<3>(jobs, hdr, counter, grid, noise, ty, bin8, s);
-        case 4: return launch_batched_nv<4>(jobs, hdr, counter, grid, noise, ty, bin8, s);
-        case 5: return launch_batched_nv<5>(jobs, hdr, counter, grid, noise, ty, bin8, s);
-        case 6: return launch_batched_nv<6>(jobs, hdr, counter, grid, noise, ty, bin8, s);
-        case 7: return launch_batched_nv<7>(jobs, hdr, counter, grid, noise, ty, bin8, s);
-        case 8: return launch_batched_nv<8>(jobs, hdr, counter, grid, noise, ty, bin8, s);
+        case 1: return launch_batched_nv<1>(L, counter, grid, noise, ty, bin8, s);
+        case 2: return launch_batched_nv<2>(L, counter, grid, noise, ty, bin8, s);
+        case 3: return launch_batched_nv<3>(L, counter, grid, noise, ty, bin8, s);
+        case 4: return launch_batched_nv<4>(L, counter, grid, noise, ty, bin8, s);
+        case 5: return launch_batched_nv<5>(L, counter, grid, noise, ty, bin8, s);
+        case 6: return launch_batched_nv<6>(L, counter, grid, noise, ty, bin8, s);
+        case 7: return launch_batched_nv<7>(L, counter, grid, noise, ty, bin8, s);
+        case 8: return launch_batched_nv<8>(L, counter, grid, noise, ty, bin8, s);
         default: return cudaErrorInvalidValue;
     }
 }

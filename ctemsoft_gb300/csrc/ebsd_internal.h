@@ -64,15 +64,13 @@ struct VjpParams {
     int opc;             // orientations per CTA
 };
 
-// Batched pattern loop (ebsd_forward.cu): a table of jobs in device memory.
-// A queued job runs at its handle's tile height (32 x 4, 8 or 16 pixels,
-// raised until binned records hold whole blocks); 8x8-binned jobs (BIN8)
-// take 8 or 16 rows.
+// Batched pattern loop (ebsd_forward.cu).  A queued job runs at its
+// handle's tile height (32 x 4, 8 or 16 pixels, raised until binned records
+// hold whole blocks); 8x8-binned jobs (BIN8) take 8 or 16 rows.
 inline bool batch_shape_ok(int ty, bool bin8)
 {
     return (ty == 4 && !bin8) || ty == 8 || ty == 16;
 }
-constexpr int kBatchMaxJobsSmem = 512;  // job starts cached in shared memory
 
 struct BatchJob {
     FwdParams p;            // detector, master, quats, out, epilogue of the job
@@ -81,10 +79,16 @@ struct BatchJob {
     long long items;        // ntiles * ceil(n / opc)
 };
 
-struct BatchHeader {
-    long long total_items;
+// One launch of the persistent queue kernel: its jobs travel in the kernel's
+// parameters (the constant bank, read through the constant cache; a kernel
+// takes up to 32 764 bytes of parameters), at most kBatchLaunchJobs of them.
+constexpr int kBatchLaunchJobs = 128;
+struct BatchLaunch {
+    long long total_items;  // items of all jobs, in job order
     int njobs, pad;
+    BatchJob job[kBatchLaunchJobs];
 };
+static_assert(sizeof(BatchLaunch) + 8 <= 32764, "kernel parameters above the 32 KB limit");
 
 // Launch configuration picked by the tuner or by default.
 struct LaunchCfg {
@@ -175,9 +179,8 @@ int64_t forward_ctas(const FwdParams& p, const LaunchCfg& cfg);
 // cells: the diagnostic instantiation that also stores p.nix/niy/ixy0/ixy1.
 cudaError_t launch_forward(const FwdParams& p, int NV, const LaunchCfg& cfg, cudaStream_t s,
                            bool cells = false);
-cudaError_t launch_forward_batched(const BatchJob* jobs, const BatchHeader* hdr,
-                                   unsigned long long* counter, int NV, bool noise, int ty,
-                                   bool bin8, int grid, cudaStream_t s);
+cudaError_t launch_forward_batched(const BatchLaunch& L, unsigned long long* counter, int NV,
+                                   bool noise, int ty, bool bin8, int grid, cudaStream_t s);
 int batched_grid(int NV, bool noise, int ty, bool bin8);
 
 // Cubochoric fundamental-zone sampling (ebsd_so3.cu).  Constants of

@@ -238,10 +238,11 @@ int ebsd_autotune(ebsd_handle* h, const ebsd_epilogue* e, int64_t n_sample,
  * run of orientations) items consumed by a persistent grid (one launch per
  * energy-bin count, noise and tile height); EBSD_BATCH_QUEUE_ALL puts every
  * job in the queue.  With EBSD_BATCH_GRAPH all of it
- * (table upload, queue reset, launches) is captured in a CUDA graph on first
- * use and replayed for later batches with the same queue shape and the same
- * large-job parameters.  Runs on h's stream; returns when the work is
- * queued.  Records equal those of ebsd_forward on the source handles. */
+ * (queue reset, launches) is captured in a CUDA graph on first use and
+ * replayed for later batches with the same job list (the same buffers, sizes
+ * and epilogues: new contents of the buffers are picked up).  Runs on h's
+ * stream; returns when the work is queued.  Records equal those of
+ * ebsd_forward on the source handles. */
 int ebsd_forward_batched(ebsd_handle* h, const ebsd_job* jobs, int32_t njobs, int32_t flags);
 
 /* Adjoint modes of ebsd_vjp. */
