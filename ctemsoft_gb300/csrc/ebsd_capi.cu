@@ -1217,9 +1217,15 @@ extern "C" int ebsd_gn_accumulate(ebsd_handle* h, const float* quats, int64_t n,
     vp.dW = h->d_dW;
     vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
     vp.opc = h->gn_opc;
-    // the Gauss-Newton kernel's CTA is 32 x tile_y threads (at most 8 rows)
-    const int ty_opt = h->vjp_tile_y > 0 ? std::min(h->vjp_tile_y, 8) : 4;
-    const int tile_y = vp.binning > ty_opt ? 8 : ty_opt;
+    // records binned 2x2 or 4x4: 32 x 16 tiles by default (four pixel rows
+    // per thread); otherwise a CTA of 32 x tile_y threads, at most 8 rows
+    int tile_y;
+    if (vp.binning == 2 || vp.binning == 4) {
+        tile_y = h->vjp_tile_y > 0 ? h->vjp_tile_y : 16;
+    } else {
+        const int ty_opt = h->vjp_tile_y > 0 ? std::min(h->vjp_tile_y, 8) : 4;
+        tile_y = vp.binning > ty_opt ? 8 : ty_opt;
+    }
     if (vp.binning > tile_y)
         return set_err(h, EBSD_EUNSUPPORTED, "Gauss-Newton: binning %d exceeds the tile",
                        vp.binning);

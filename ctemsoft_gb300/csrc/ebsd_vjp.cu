@@ -513,6 +513,108 @@ __global__ void __launch_bounds__(256, EBSD_GN_MIN_BLOCKS) k_gn(const FwdParams 
     }
 }
 
+// Gauss-Newton for records binned 2x2 or 4x4: CTAs of four warps over 32 x 4
+// PPT pixel tiles, PPT pixel rows (layers of 32 x 4) per thread.  Per layer
+// the warp sums each binning block's value and Jacobian by shuffles (as
+// k_gn), and the block's first lane stores the block's eight numbers (J_B,
+// O_B, T_B) in shared memory; after the last layer every lane forms one or
+// two of the 36 products (21 of J J^T, J T, J O and the three dot products),
+// summed over the warp's blocks of all layers.  The products are paid once
+// per block instead of in every lane, and no warp reduction of the 36 sums
+// is needed.
+#ifndef EBSD_GN1_MIN_BLOCKS
+#define EBSD_GN1_MIN_BLOCKS 5
+#endif
+template <int NV, int PPT>
+__global__ void __launch_bounds__(128, EBSD_GN1_MIN_BLOCKS)
+    k_gn1(const FwdParams prm, const VjpParams vp, int tiles_x, int ntiles, int opc)
+{
+    extern __shared__ float sm[];  // [opc][4 warps][36] warp sums, then per warp the blocks
+    const int b = vp.binning;      // 2 or 4
+    const int bpw = 32 / (b * b);  // binning blocks per warp and layer
+    float* red = sm;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    float* blk = sm + (size_t)opc * 4 * kGnK + (size_t)wid * PPT * 8 * 8;  // [PPT * bpw][8]
+    int tx, ty;
+    adj_pixel<true>(tid, b, tx, ty);
+    const int bw = 32 / b;         // warp width in pixels
+    const bool leader = (lane % bw) % b == 0 && (lane / bw) % b == 0;
+    const int bidx = (lane % bw) / b;  // block of this lane within the warp's layer
+    // the products this lane forms: operands (0..5 J_B, 6 O_B, 7 T_B) of
+    // product j = lane and j = lane + 32, in the order of the partial sums
+    auto operands = [](int j, int& u, int& v) {
+        if (j < 6) {
+            u = 7; v = j;
+        } else if (j < 12) {
+            u = 6; v = j - 6;
+        } else if (j < 15) {
+            u = j == 14 ? 7 : 6; v = j == 12 ? 6 : 7;
+        } else {
+            int k = j - 15, i = 0;
+            while (k >= 6 - i) { k -= 6 - i; ++i; }
+            u = i; v = i + k;
+        }
+    };
+    int u0, v0, u1 = 0, v1 = 0;
+    operands(lane, u0, v0);
+    const bool two = lane + 32 < kGnK;
+    if (two) operands(lane + 32, u1, v1);
+
+    const unsigned n_ob = (unsigned)((prm.n + opc - 1) / opc);
+    const int t = (int)(blockIdx.x / n_ob);
+    const int64_t o_begin = (int64_t)(blockIdx.x % n_ob) * opc;
+    const int x = (t % tiles_x) * kTileX + tx;
+    const int y0 = (t / tiles_x) * (4 * PPT) + ty;
+    const uint64_t pol = l2_policy_evict_last();
+    const float pref = (float)prm.prefactor;
+    const float ib2 = 1.0f / (float)(b * b);
+    const int64_t rec = (int64_t)prm.out_nx * prm.out_ny;
+    const int nblk = PPT * bpw;
+
+    for (int64_t o = o_begin; o < o_begin + opc && o < prm.n; ++o) {
+#pragma unroll 1
+        for (int k = 0; k < PPT; ++k) {
+            const int y = y0 + 4 * k;
+            // only pixels of full output blocks contribute (binning crops to the floor)
+            const bool inside = x < prm.numsx && y < prm.numsy && x < prm.out_nx * b &&
+                                y < prm.out_ny * b;
+            float val = 0.0f, J[6] = {0, 0, 0, 0, 0, 0};
+            if (inside) pixel_value_jacobian<NV>(prm, vp, y * prm.numsx + x, o, pol, pref, val, J);
+            const float O = adj_block_sum(val, b) * ib2;
+            float JB[6];
+#pragma unroll
+            for (int a = 0; a < 6; ++a) JB[a] = adj_block_sum(J[a], b) * ib2;
+            if (leader) {
+                // a block lies wholly inside or wholly outside (then all zeros)
+                const float dv =
+                    inside ? vp.data[o * rec + (int64_t)(y / b) * prm.out_nx + x / b] : 0.0f;
+                float4* e = reinterpret_cast<float4*>(blk + (k * bpw + bidx) * 8);
+                e[0] = make_float4(JB[0], JB[1], JB[2], JB[3]);
+                e[1] = make_float4(JB[4], JB[5], O, dv);
+            }
+        }
+        __syncwarp();
+        float s0 = 0.0f, s1 = 0.0f;
+        for (int i = 0; i < nblk; ++i) {
+            const float* e = blk + i * 8;
+            s0 = fmaf(e[u0], e[v0], s0);
+            if (two) s1 = fmaf(e[u1], e[v1], s1);
+        }
+        float* rw = red + ((o - o_begin) * 4 + wid) * kGnK;
+        rw[lane] = s0;
+        if (two) rw[lane + 32] = s1;
+        __syncwarp();  // the blocks of the next orientation overwrite these
+    }
+    __syncthreads();
+    const int no = (int)min((int64_t)opc, prm.n - o_begin);
+    for (int i = tid; i < no * kGnK; i += blockDim.x) {
+        const int ol = i / kGnK, k = i - ol * kGnK;
+        float s2 = 0.0f;
+        for (int w = 0; w < 4; ++w) s2 += red[(ol * 4 + w) * kGnK + k];
+        vp.partial[((o_begin + ol) * ntiles + t) * kGnK + k] = s2;
+    }
+}
+
 // Per orientation: binary64 sums of the partials, then H, g and the loss.
 __global__ void k_gn_reduce(const float* __restrict__ partial, int64_t n, int ntiles,
                             double* __restrict__ sys, float* __restrict__ loss)
@@ -684,6 +786,26 @@ cudaError_t allow_smem(Kern kern, size_t bytes)
 template <int NV>
 cudaError_t launch_gn_nv(const FwdParams& p, const VjpParams& vp, int tile_y, cudaStream_t s)
 {
+    if ((vp.binning == 2 || vp.binning == 4) && tile_y % 4 == 0 && tile_y <= 32) {
+        // binned 2x2 / 4x4: four warps, tile_y / 4 pixel rows per thread
+        const int tiles_x = (p.numsx + kTileX - 1) / kTileX;
+        const int ntiles = tiles_x * ((p.numsy + tile_y - 1) / tile_y);
+        const int opc = vp.opc;
+        const int64_t blocks = ((p.n + opc - 1) / opc) * ntiles;
+        if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+        const int ppt = tile_y / 4;
+        const size_t smem = sizeof(float) * ((size_t)opc * 4 * kGnK + (size_t)4 * ppt * 64);
+        auto go = [&](auto kern) {
+            const cudaError_t e = allow_smem(kern, smem);
+            if (e != cudaSuccess) return e;
+            kern<<<(unsigned)blocks, 128, smem, s>>>(p, vp, tiles_x, ntiles, opc);
+            return cudaGetLastError();
+        };
+        return ppt == 1   ? go(k_gn1<NV, 1>)
+               : ppt == 2 ? go(k_gn1<NV, 2>)
+               : ppt == 4 ? go(k_gn1<NV, 4>)
+                          : go(k_gn1<NV, 8>);
+    }
     const int tiles_x = (p.numsx + kTileX - 1) / kTileX;
     const int tiles_y = (p.numsy + tile_y - 1) / tile_y;
     const int ntiles = tiles_x * tiles_y;

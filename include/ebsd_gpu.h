@@ -125,11 +125,12 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    halved while the launch would have fewer than 32 CTAs
  *                    per SM.
  *   "vjp_tile_y"     tile height in pixels of ebsd_vjp and the Gauss-Newton
- *                    kernels: 4, 8, 16 or 32.  Unbinned adjoint records: 16 by
- *                    default (CTAs of 128 threads, tile_y / 4 pixels per
- *                    thread).  Binned records and Gauss-Newton: 4 by
- *                    default, at most 8 (one thread per pixel); binning 8
- *                    always uses 8.
+ *                    kernels: 4, 8, 16 or 32.  Unbinned adjoint records and
+ *                    Gauss-Newton on records binned 2x2 or 4x4: 16 by
+ *                    default (CTAs of 128 threads, tile_y / 4 pixel rows per
+ *                    thread).  Binned adjoint records and the other
+ *                    Gauss-Newton cases: 4 by default, at most 8 (one thread
+ *                    per pixel); binning 8 always uses 8.
  *   "noise_index_offset"  the pattern index of the first orientation of the
  *                    next calls (default 0): Poisson noise is keyed by (seed,
  *                    pattern index, pixel), so a caller that computes a long
