@@ -131,7 +131,7 @@ struct ebsd_handle {
     int mc_fp32 = 0;     // Monte-Carlo trajectories in binary32
     int host_direct = 1; // kernel stores straight into pinned host outputs
     int vjp_tile_y = 0;  // adjoint / Gauss-Newton tile height; 0: the defaults below
-    int vjp_opc = 8;     // adjoint orientations per CTA
+    int vjp_opc = 0;     // adjoint orientations per CTA; 0: 16 unbinned, 8 binned
     int gn_opc = 32;     // Gauss-Newton orientations per CTA
     int weights_fp64 = 1;
     int lambert_accurate = 0;
@@ -978,7 +978,7 @@ extern "C" int ebsd_vjp(ebsd_handle* h, const float* quats, int64_t n, const ebs
     vp.drg = h->d_drg;
     vp.dW = h->d_dW;
     vp.binning = e->scalingmode == EBSD_SCALING_NOT ? 1 : e->binning;
-    vp.opc = h->vjp_opc;
+    vp.opc = h->vjp_opc > 0 ? h->vjp_opc : (vp.binning == 1 ? 16 : 8);
     // unbinned records: 32 x 16 tiles by default (tile_y / 4 pixels per
     // thread); binned ones a CTA of 32 x tile_y threads, at most 8 rows
     int tile_y = h->vjp_tile_y > 0 ? h->vjp_tile_y : (vp.binning == 1 ? 16 : 4);

@@ -136,7 +136,8 @@ int ebsd_set_stream(ebsd_handle* h, void* stream);
  *                    pattern index, pixel), so a caller that computes a long
  *                    orientation list in pieces sets the piece's start here
  *                    and gets the noise of one call over the whole list.
- *   "vjp_orient_per_cta"  ebsd_vjp's orientations per CTA, 1..64 (default 8).
+ *   "vjp_orient_per_cta"  ebsd_vjp's orientations per CTA, 1..64 (default 16
+ *                    for unbinned records, 8 for binned ones).
  *                    (ebsd_vjp_noalloc keeps 8 and 2, the shape its size
  *                    limit is stated for.)
  *   "gn_orient_per_cta"   the Gauss-Newton kernels', 1..64 (default 32: 3 %

@@ -96,6 +96,31 @@ def test_refine_orientations_and_centre(built):
     assert mis.max() < 0.01
 
 
+@pytest.mark.parametrize("binning", [2, 4])
+def test_accumulation_is_the_same_at_every_tile_shape(built, binning):
+    """The Gauss-Newton accumulation for 2x2 / 4x4-binned records at each tile
+    height (1, 2, 4 and 8 pixel rows per thread) and orientations per CTA:
+    the pattern-centre system and the losses agree with the default shape's
+    to rounding, on a detector with partial tiles."""
+    torch = pytest.importorskip("torch")
+    wl, h, epi, qt, targets, _ = _problem(torch, binning, n=19, size=(100, 76))
+    rng = np.random.default_rng(3)
+    q0 = torch.from_numpy(perturb(qt, 0.5, rng)).cuda()
+    ref = None
+    for tile_y, opc in [(16, 32), (4, 1), (8, 7), (32, 5)]:
+        h.set_option("vjp_tile_y", tile_y)
+        h.set_option("gn_orient_per_cta", opc)
+        loss = torch.zeros(len(qt), device="cuda")
+        sysc = h.gn_accumulate(q0, epi, targets, 1e-3, pc_system=True, loss=loss)
+        cur = (sysc, loss.cpu().numpy().astype(np.float64))
+        if ref is None:
+            ref = cur
+            continue
+        scale = np.abs(ref[0]).max()
+        assert np.abs(cur[0] - ref[0]).max() <= 1e-4 * scale, (tile_y, opc, cur[0], ref[0])
+        np.testing.assert_allclose(cur[1], ref[1], rtol=1e-4, atol=1e-9)
+
+
 def test_two_phase_api_matches_refine(built):
     """ebsd_gn_accumulate + host solve + ebsd_gn_apply (the multi-GPU form)
     takes the same step as one iteration of ebsd_refine."""

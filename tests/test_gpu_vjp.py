@@ -88,6 +88,34 @@ def test_ragged_detector_matches_fp64_analytic(built, binning):
     h.close()
 
 
+@pytest.mark.parametrize("tile_y,opc", [(4, 1), (8, 3), (16, 16), (32, 5)])
+@pytest.mark.parametrize("mode", ["ndp", "cot"])
+def test_every_unbinned_tile_shape_matches_fp64_analytic(built, tile_y, opc, mode):
+    """The unbinned adjoint at each tile height (1, 2, 4 and 8 pixel rows per
+    thread) and odd orientation counts per CTA, on the ragged 70 x 45
+    detector (partial tiles), against the oracle's binary64 gradient."""
+    from oracle import oracle as O
+    wl = synth.tiny(seed=5, numsx=70, numsy=45, npx=60, nE=5, mc_nsx=80, n_orient=7)
+    wl.delta = 110.0
+    sr, acc = wl.master(), wl.mc()
+    q = wl.quaternions()
+    h, pref = _handle(wl, sr, acc)
+    h.set_option("vjp_tile_y", tile_y)
+    h.set_option("vjp_orient_per_cta", opc)
+    if mode == "ndp":
+        data = _targets(O, wl, sr, acc, q, 1)
+    else:
+        data = np.random.default_rng(1).standard_normal((len(q), 45, 70)).astype(np.float32)
+    loss, g = h.vjp(q, capi.epilogue(pref), data, mode)
+    rloss, rg = O.vjp_f64(wl.geometry(), acc, 1, wl.nEbins, sr, q, pref, 1, mode, data)
+    if mode == "ndp":
+        np.testing.assert_allclose(loss, rloss, rtol=TOL_LOSS, atol=1e-7)
+    err = _grad_err(g, rg)
+    print("tile", tile_y, "opc", opc, mode, "grad rel err (rot, xpc, ypc, L):", err)
+    assert (err < TOL_GRAD).all(), err
+    h.close()
+
+
 def test_cotangent_matches_fp64_analytic(built):
     from oracle import oracle as O
     wl = _wl()
