@@ -76,6 +76,124 @@ __device__ __forceinline__ float adj_block_sum(float v, int b)
     return v;
 }
 
+// Per-orientation geometry of one pixel for the adjoint: the rotated
+// direction d, its normalised and folded h (fold sign s, 1/|d| ind), the
+// Lambert point's Jacobian rows dX, dY, and the cell and bilinear fractions.
+struct AdjGeom {
+    float d0, d1, d2, h0, h1, h2, s, ind;
+    float dX[3], dY[3];
+    int ix0, iy0;
+    float dx, dy;
+};
+
+__device__ __forceinline__ void adj_geometry(const FwdParams& prm, const float4 q, const float4 r,
+                                             AdjGeom& g)
+{
+    rotate_direction(q, r.x, r.y, r.z, g.d0, g.d1, g.d2);
+    // normalisation and fold (:588-589) with the hardware reciprocal square
+    // root: the adjoint needs relative accuracy, not the reference's rounding
+    g.ind = rsqrtf(fmaf(g.d0, g.d0, fmaf(g.d1, g.d1, g.d2 * g.d2)));
+    g.h0 = g.d0 * g.ind;
+    g.h1 = g.d1 * g.ind;
+    g.h2 = g.d2 * g.ind;
+    g.s = g.h2 < 0.0f ? -1.0f : 1.0f;
+    float LX, LY;
+    lambert_inverse_jac(g.s * g.h0, g.s * g.h1, g.s * g.h2, prm.spi2, LX, LY, g.dX, g.dY);
+    int nix, niy;
+    g.ix0 = lambert_cell(prm.scl * LX, prm.npx, g.dx, nix);
+    g.iy0 = lambert_cell(prm.scl * LY, prm.npy, g.dy, niy);
+}
+
+// The four weighted corner sums SA = sum_k W_k A_k ... SD of the gather and
+// the weight-slope sums U0 = sum_k G0_k bv_k, U1 = sum_k G1_k bv_k (bv_k the
+// per-bin bilinear value): S = (SA, SB, SC, SD, U0, U1).  P and both
+// bilinear slopes follow from SA..SD with four FMAs per bin, and since
+// dW_k/dtheta_a = G0_k di0_a + G1_k di1_a the weight terms need only U0, U1.
+// The sums run on packed pairs of bins (even bins in the low halves, odd in
+// the high), two fused multiply-adds per instruction.
+template <int NV>
+__device__ __forceinline__ void adj_gather(const FwdParams& prm, const VjpParams& vp, int p,
+                                           uint64_t pol, const AdjGeom& g, float (&S)[6])
+{
+    const int ix1 = min(g.ix0 + 1, 2 * prm.npx), iy1 = min(g.iy0 + 1, 2 * prm.npy);
+    // node offsets in 32 bits: ebsd_set_master keeps the master below 2^31 float4
+    const float4* m00 = prm.master + (uint32_t)(g.iy0 * prm.gx + g.ix0) * (uint32_t)NV;
+    const int col = (ix1 - g.ix0) * NV;             // 0 at the grid's last column
+    const int row = (iy1 - g.iy0) * prm.gx * NV;    // 0 at its last row
+    const float dxm = 1.0f - g.dx, dym = 1.0f - g.dy;
+    const float w00 = dxm * dym, w10 = g.dx * dym, w01 = dxm * g.dy, w11 = g.dx * g.dy;
+    const f2_t W00 = f2_pack(w00, w00), W10 = f2_pack(w10, w10), W01 = f2_pack(w01, w01),
+               W11 = f2_pack(w11, w11);
+    f2_t acc[6] = {0, 0, 0, 0, 0, 0};  // +0.0f pairs
+    const float4* wp = prm.W + p;      // plane c of W at wp + c P
+    const float4* ep = vp.dW + p;      // plane c of G0; G1 NV planes further
+    const int64_t plane = prm.P, eplane = (int64_t)NV * prm.P;
+    // one float4 group of bins at a time: unrolling would hoist all the
+    // vector loads and spill
+#pragma unroll 1
+    for (int c = 0; c < NV; ++c, wp += plane, ep += plane) {
+        f2_t A[2], B[2], C[2], D[2], wc[2], e0[2], e1[2];
+        const float4* m = m00 + c;
+        ldg4_keep2(m, pol, A[0], A[1]);
+        ldg4_keep2(m + col, pol, B[0], B[1]);
+        ldg4_keep2(m + row, pol, C[0], C[1]);
+        ldg4_keep2(m + row + col, pol, D[0], D[1]);
+        ldg4_keep2(wp, pol, wc[0], wc[1]);
+        ldg4_keep2(ep, pol, e0[0], e0[1]);
+        ldg4_keep2(ep + eplane, pol, e1[0], e1[1]);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const f2_t bv = f2_fma(A[h], W00, f2_fma(B[h], W10, f2_fma(C[h], W01, f2_mul(D[h], W11))));
+            acc[0] = f2_fma(wc[h], A[h], acc[0]);
+            acc[1] = f2_fma(wc[h], B[h], acc[1]);
+            acc[2] = f2_fma(wc[h], C[h], acc[2]);
+            acc[3] = f2_fma(wc[h], D[h], acc[3]);
+            acc[4] = f2_fma(e0[h], bv, acc[4]);
+            acc[5] = f2_fma(e1[h], bv, acc[5]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) S[i] = f2_sum(acc[i]);
+}
+
+// Value and the six derivatives of one orientation from its geometry and
+// gather sums; t0..t2 are the drg planes (d rg/d(xpc, ypc, L), with d Dx/d
+// theta in .w) and di1 the plane of d Dy/d theta.
+__device__ __forceinline__ void adj_finish(const FwdParams& prm, const float4 q, const AdjGeom& g,
+                                           const float (&S)[6], const float4 t0, const float4 t1,
+                                           const float4 t2, const float4 di1, float pref,
+                                           float& val, float (&J)[6])
+{
+    const float SA = S[0], SB = S[1], SC = S[2], SD = S[3], U0 = S[4], U1 = S[5];
+    const float dxm = 1.0f - g.dx, dym = 1.0f - g.dy;
+    const float w00 = dxm * dym, w10 = g.dx * dym, w01 = dxm * g.dy, w11 = g.dx * g.dy;
+    const float P = fmaf(SA, w00, fmaf(SB, w10, fmaf(SC, w01, SD * w11)));
+    const float gX = fmaf(SB - SA, dym, (SD - SC) * g.dy);
+    const float gY = fmaf(SC - SA, dxm, (SD - SB) * g.dx);
+    val = pref * P;
+    const float sx = prm.scl * pref * gX, sy = prm.scl * pref * gY;
+    const float gc0 = sx * g.dX[0] + sy * g.dY[0];
+    const float gc1 = sx * g.dX[1] + sy * g.dY[1];
+    const float gc2 = sx * g.dX[2] + sy * g.dY[2];
+    const float pr = gc0 * g.h0 + gc1 * g.h1 + gc2 * g.h2;
+    const float k = g.s * g.ind;
+    const float g0 = k * (gc0 - pr * g.h0), g1 = k * (gc1 - pr * g.h1), g2 = k * (gc2 - pr * g.h2);
+    J[0] = g.d1 * g2 - g.d2 * g1;
+    J[1] = g.d2 * g0 - g.d0 * g2;
+    J[2] = g.d0 * g1 - g.d1 * g0;
+    // M^T g = conj(q) (x) (0,g) (x) q
+    const float u0 = -(g0 * q.y) - g1 * q.z - g2 * q.w;
+    const float u1 = g0 * q.x + g1 * q.w - g2 * q.z;
+    const float u2 = -(g0 * q.w) + g1 * q.x + g2 * q.y;
+    const float u3 = g0 * q.z - g1 * q.y + g2 * q.x;
+    const float m0 = q.x * u1 - q.y * u0 - q.z * u3 + q.w * u2;
+    const float m1 = q.x * u2 + q.y * u3 - q.z * u0 - q.w * u1;
+    const float m2 = q.x * u3 - q.y * u2 + q.z * u1 - q.w * u0;
+    J[3] = m0 * t0.x + m1 * t0.y + m2 * t0.z + pref * fmaf(U0, t0.w, U1 * di1.x);
+    J[4] = m0 * t1.x + m1 * t1.y + m2 * t1.z + pref * fmaf(U0, t1.w, U1 * di1.y);
+    J[5] = m0 * t2.x + m1 * t2.y + m2 * t2.z + pref * fmaf(U0, t2.w, U1 * di1.z);
+}
+
 // Value and the six derivatives (w0, w1, w2, xpc, ypc, L) of output pixel p
 // of orientation o, before binning.
 template <int NV>
@@ -85,93 +203,15 @@ __device__ __forceinline__ void pixel_value_jacobian(const FwdParams& prm, const
 {
     const float4 q = __ldg(prm.quats + o);
     const float4 r = ldg4_keep(prm.rg + p, pol);
-    float d0, d1, d2;
-    rotate_direction(q, r.x, r.y, r.z, d0, d1, d2);
-    // normalisation and fold (:588-589) with the hardware reciprocal square
-    // root: the adjoint needs relative accuracy, not the reference's rounding
-    const float ind = rsqrtf(fmaf(d0, d0, fmaf(d1, d1, d2 * d2)));
-    const float h0 = d0 * ind, h1 = d1 * ind, h2 = d2 * ind;
-    const float s = h2 < 0.0f ? -1.0f : 1.0f;
-    float LX, LY, dX[3], dY[3];
-    lambert_inverse_jac(s * h0, s * h1, s * h2, prm.spi2, LX, LY, dX, dY);
-    float dx, dy;
-    int nix, niy;
-    const int ix0 = lambert_cell(prm.scl * LX, prm.npx, dx, nix);
-    const int iy0 = lambert_cell(prm.scl * LY, prm.npy, dy, niy);
-    const int ix1 = min(ix0 + 1, 2 * prm.npx), iy1 = min(iy0 + 1, 2 * prm.npy);
-    const float dxm = 1.0f - dx, dym = 1.0f - dy;
-    // node offsets in 32 bits: ebsd_set_master keeps the master below 2^31 float4
-    const float4* m00 = prm.master + (uint32_t)(iy0 * prm.gx + ix0) * (uint32_t)NV;
-    const float4* m10 = prm.master + (uint32_t)(iy0 * prm.gx + ix1) * (uint32_t)NV;
-    const float4* m01 = prm.master + (uint32_t)(iy1 * prm.gx + ix0) * (uint32_t)NV;
-    const float4* m11 = prm.master + (uint32_t)(iy1 * prm.gx + ix1) * (uint32_t)NV;
-    // Weighted corner sums SA = sum_k W_k A_k etc. give P and both bilinear
-    // slopes with four FMAs per bin; the weight derivatives need the
-    // per-bin bilinear value bv.
-    const float w00 = dxm * dym, w10 = dx * dym, w01 = dxm * dy, w11 = dx * dy;
-    // The sums run on packed pairs of bins (even bins in the low halves,
-    // odd in the high), two fused multiply-adds per instruction.
-    const f2_t W00 = f2_pack(w00, w00), W10 = f2_pack(w10, w10), W01 = f2_pack(w01, w01),
-               W11 = f2_pack(w11, w11);
-    f2_t pA = 0, pB = 0, pC = 0, pD = 0, pU0 = 0, pU1 = 0;  // +0.0f pairs
-    // one float4 group of bins at a time: unrolling would hoist all
-    // 8*NV vector loads and spill
-    // dW_k/dtheta_a = G0_k di0_a + G1_k di1_a, so the weight terms need only
-    // U0 = sum_k G0_k bv_k and U1 = sum_k G1_k bv_k
-    const float4* wp = prm.W + p;           // plane c of W at wp + c P
-    const float4* ep = vp.dW + p;           // plane c of G0; G1 NV planes further
-    const int64_t plane = prm.P, eplane = (int64_t)NV * prm.P;
-#pragma unroll 1
-    for (int c = 0; c < NV; ++c, wp += plane, ep += plane) {
-        f2_t A[2], B[2], C[2], D[2], wc[2], e0[2], e1[2];
-        ldg4_keep2(m00 + c, pol, A[0], A[1]);
-        ldg4_keep2(m10 + c, pol, B[0], B[1]);
-        ldg4_keep2(m01 + c, pol, C[0], C[1]);
-        ldg4_keep2(m11 + c, pol, D[0], D[1]);
-        ldg4_keep2(wp, pol, wc[0], wc[1]);
-        ldg4_keep2(ep, pol, e0[0], e0[1]);
-        ldg4_keep2(ep + eplane, pol, e1[0], e1[1]);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const f2_t bv = f2_fma(A[h], W00, f2_fma(B[h], W10, f2_fma(C[h], W01, f2_mul(D[h], W11))));
-            pA = f2_fma(wc[h], A[h], pA);
-            pB = f2_fma(wc[h], B[h], pB);
-            pC = f2_fma(wc[h], C[h], pC);
-            pD = f2_fma(wc[h], D[h], pD);
-            pU0 = f2_fma(e0[h], bv, pU0);
-            pU1 = f2_fma(e1[h], bv, pU1);
-        }
-    }
-    const float SA = f2_sum(pA), SB = f2_sum(pB), SC = f2_sum(pC), SD = f2_sum(pD);
-    const float U0 = f2_sum(pU0), U1 = f2_sum(pU1);
-    const float P = fmaf(SA, w00, fmaf(SB, w10, fmaf(SC, w01, SD * w11)));
-    const float gX = fmaf(SB - SA, dym, (SD - SC) * dy);
-    const float gY = fmaf(SC - SA, dxm, (SD - SB) * dx);
-    val = pref * P;
-    const float sx = prm.scl * pref * gX, sy = prm.scl * pref * gY;
-    const float gc0 = sx * dX[0] + sy * dY[0];
-    const float gc1 = sx * dX[1] + sy * dY[1];
-    const float gc2 = sx * dX[2] + sy * dY[2];
-    const float pr = gc0 * h0 + gc1 * h1 + gc2 * h2;
-    const float k = s * ind;
-    const float g0 = k * (gc0 - pr * h0), g1 = k * (gc1 - pr * h1), g2 = k * (gc2 - pr * h2);
-    J[0] = d1 * g2 - d2 * g1;
-    J[1] = d2 * g0 - d0 * g2;
-    J[2] = d0 * g1 - d1 * g0;
-    // M^T g = conj(q) (x) (0,g) (x) q
-    const float u0 = -(g0 * q.y) - g1 * q.z - g2 * q.w;
-    const float u1 = g0 * q.x + g1 * q.w - g2 * q.z;
-    const float u2 = -(g0 * q.w) + g1 * q.x + g2 * q.y;
-    const float u3 = g0 * q.z - g1 * q.y + g2 * q.x;
-    const float m0 = q.x * u1 - q.y * u0 - q.z * u3 + q.w * u2;
-    const float m1 = q.x * u2 + q.y * u3 - q.z * u0 - q.w * u1;
-    const float m2 = q.x * u3 - q.y * u2 + q.z * u1 - q.w * u0;
-    const float4 r0 = ldg4_keep(vp.drg + p, pol), r1 = ldg4_keep(vp.drg + prm.P + p, pol),
-                 r2 = ldg4_keep(vp.drg + 2 * (int64_t)prm.P + p, pol);
+    AdjGeom g;
+    adj_geometry(prm, q, r, g);
+    float S[6];
+    adj_gather<NV>(prm, vp, p, pol, g, S);
+    const int64_t eplane = (int64_t)NV * prm.P;
+    const float4 t0 = ldg4_keep(vp.drg + p, pol), t1 = ldg4_keep(vp.drg + prm.P + p, pol),
+                 t2 = ldg4_keep(vp.drg + 2 * (int64_t)prm.P + p, pol);
     const float4 di1 = ldg4_keep(vp.dW + 2 * eplane + p, pol);  // (xpc, ypc, L)
-    J[3] = m0 * r0.x + m1 * r0.y + m2 * r0.z + pref * fmaf(U0, r0.w, U1 * di1.x);
-    J[4] = m0 * r1.x + m1 * r1.y + m2 * r1.z + pref * fmaf(U0, r1.w, U1 * di1.y);
-    J[5] = m0 * r2.x + m1 * r2.y + m2 * r2.z + pref * fmaf(U0, r2.w, U1 * di1.z);
+    adj_finish(prm, q, g, S, t0, t1, t2, di1, pref, val, J);
 }
 
 // Resident CTAs per SM the register allocation is held to (256 threads
