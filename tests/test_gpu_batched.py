@@ -186,6 +186,38 @@ def test_batched_large_jobs_run_as_own_launches(built):
     check("queue only")
 
 
+def test_batched_more_jobs_than_one_launch_carries(built):
+    """A launch of the queue kernel carries at most 128 jobs in its
+    parameters: 300 small jobs of one launch group run as three launches,
+    with their graph replayed for new orientations; records equal per-job
+    launches."""
+    torch = pytest.importorskip("torch")
+    wl = synth.tiny(seed=9, numsx=40, numsy=24, npx=40, nE=5)
+    src = capi.Handle(0)
+    src.set_master(wl.master())
+    num_el = src.set_detector(wl.geometry(), wl.mc(), 1, 5)
+    epi = capi.epilogue(capi.prefactor(15.0, 100.0, num_el), scalingmode="gam", gammavalue=0.33)
+    rng = np.random.default_rng(11)
+    jobs = []
+    for j in range(300):
+        n = int(rng.integers(1, 6))
+        q = torch.from_numpy(synth.shoemake_quaternions(n, 2000 + j)).cuda()
+        jobs.append((src, q, epi, torch.full((n, 24, 40), -1.0, device="cuda")))
+    runner = capi.Handle(0)
+    for rep in range(2):
+        if rep:
+            for j, (h, q, e, out) in enumerate(jobs):
+                q.copy_(torch.from_numpy(synth.shoemake_quaternions(q.shape[0], 5000 + j)))
+                out.fill_(-1.0)
+        runner.forward_batched(jobs, graph=True, queue_all=True)
+        torch.cuda.synchronize()
+        for i, (h, q, e, out) in enumerate(jobs):
+            ref = torch.empty_like(out)
+            h.forward(q, e, out=ref)
+            torch.cuda.synchronize()
+            assert torch.equal(out, ref), f"pass {rep} job {i}"
+
+
 @pytest.mark.parametrize("weights", ["fp64", "reference"])
 def test_c3_shaped_jobs_against_the_oracle(built, weights):
     """Jobs shaped like the 64-job batched workload, run by ebsd_forward_batched
