@@ -308,6 +308,8 @@ int fill_params(ebsd_handle* h, const ebsd_epilogue* e, FwdParams& p)
         p.binning = b;
         p.mode = e->scalingmode;
         p.gammavalue = e->gammavalue;
+        p.gamma_fast = std::isfinite(e->gammavalue) && e->gammavalue > 0.0f &&
+                       e->gammavalue != std::floor(e->gammavalue);
         const float fb = (float)b;
         p.bindx = 1.0f / (fb * fb);
         p.poisson = e->poisson;

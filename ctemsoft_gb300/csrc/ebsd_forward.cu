@@ -31,10 +31,15 @@ __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 // reference-order variant (STRICT) calls powf; the default takes the
 // hardware exp2/log2 form (__powf, a few ulps) for positive values, 6 % of
 // the kernel's time at 640x480 against parity gates of 1e-5 (FP64) and
-// 1e-4 (reference).
+// 1e-4 (reference).  fast: the exponent is positive, finite and not an
+// integer (the launch's own flag, e.g. the reference's 0.33), for which
+// __powf has powf's special values for every x (+-0 -> +0, x < 0 -> NaN,
+// +inf -> +inf, NaN -> NaN), so no per-pixel test is needed: the test and
+// its powf fallback cost 2.8 % at 640x480.
 template <bool STRICT>
-__device__ __forceinline__ float gamma_pow(float x, float g)
+__device__ __forceinline__ float gamma_pow(float x, float g, bool fast)
 {
+    if (!STRICT && fast) return __powf(x, g);
     if (!STRICT && x > 0.0f) return __powf(x, g);
     return powf(x, g);
 }
@@ -293,14 +298,16 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
             }
         }
         if (!binned) {
-            if (prm.mode == EBSD_SCALING_GAM) val = gamma_pow<STRICT>(val, prm.gammavalue);
+            if (prm.mode == EBSD_SCALING_GAM)
+                val = gamma_pow<STRICT>(val, prm.gammavalue, prm.gamma_fast);
             if (inside) __stcs(prm.out + o * rec + p, val);
         } else if (b <= 4) {
             // whole blocks within the warp: no CTA barrier
             float s = b == 2 ? block_sum<2, STRICT>(val, lane) : block_sum<4, STRICT>(val, lane);
             if (lane < bw && (lane & (b - 1)) == 0) {                        // top-left lanes
                 s = s * prm.bindx;                                           // :640
-                if (prm.mode == EBSD_SCALING_GAM) s = gamma_pow<STRICT>(s, prm.gammavalue);
+                if (prm.mode == EBSD_SCALING_GAM)
+                    s = gamma_pow<STRICT>(s, prm.gammavalue, prm.gamma_fast);
                 const int X = ((t % tiles_x) * kTileX + tx) / b;
                 const int Y = ((t / tiles_x) * tile_y + ty) / b;
                 if (X < prm.out_nx && Y < prm.out_ny)
@@ -322,7 +329,8 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
             if (!(rgrp & 1) && lane == 0) {
                 float sb = sh + *slot;
                 sb = sb * prm.bindx;                                         // :640
-                if (prm.mode == EBSD_SCALING_GAM) sb = gamma_pow<false>(sb, prm.gammavalue);
+                if (prm.mode == EBSD_SCALING_GAM)
+                    sb = gamma_pow<false>(sb, prm.gammavalue, prm.gamma_fast);
                 const int X = ((t % tiles_x) * kTileX) / 8 + wid % wpr;
                 const int Y = ((t / tiles_x) * tile_y) / 8 + (rgrp >> 1);
                 if (X < prm.out_nx && Y < prm.out_ny)
@@ -337,7 +345,8 @@ __device__ __forceinline__ void forward_tile(const FwdParams& prm, int tile_y, i
                 for (int jj = 0; jj < b; ++jj)
                     for (int ii = 0; ii < b; ++ii) s = s + tile[(ty * b + jj) * 33 + tx * b + ii];
                 s = s * prm.bindx;                                           // :640
-                if (prm.mode == EBSD_SCALING_GAM) s = gamma_pow<STRICT>(s, prm.gammavalue);
+                if (prm.mode == EBSD_SCALING_GAM)
+                    s = gamma_pow<STRICT>(s, prm.gammavalue, prm.gamma_fast);
                 const int X = ((t % tiles_x) * kTileX) / b + tx;
                 const int Y = ((t / tiles_x) * tile_y) / b + ty;
                 if (X < prm.out_nx && Y < prm.out_ny)

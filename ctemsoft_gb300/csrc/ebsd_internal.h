@@ -38,6 +38,7 @@ struct FwdParams {
     float gammavalue, bindx;
     int out_nx, out_ny;
     int poisson;
+    int gamma_fast;        // 'gam' with a positive, finite, non-integer exponent (see gamma_pow)
     uint64_t seed;
     int64_t o_offset;      // index of quats[0] within the call (noise streams)
     int accurate;          // 1: cancellation-free 1 - z near the poles; 2: binary64 geometry
