@@ -236,10 +236,10 @@ int ebsd_autotune(ebsd_handle* h, const ebsd_epilogue* e, int64_t n_sample,
  * (phase); all sources must be on h's device.  A job whose own launch would
  * fill the GPU several times over (at least 64 CTAs per SM at its source
  * handle's launch shape, e.g. the autotuner's) runs as that launch; the
- * others share a device work queue of (job, 32 x 4 or 32 x 8-pixel tile,
- * run of orientations) items consumed by a persistent grid (one launch per
- * energy-bin count, noise and tile height); EBSD_BATCH_QUEUE_ALL puts every
- * job in the queue.  With EBSD_BATCH_GRAPH all of it
+ * others share a device work queue of (job, 32 x 4, 32 x 8 or 32 x 16-pixel
+ * tile at the job's tuned height, run of orientations) items consumed by a
+ * persistent grid (one launch per energy-bin count, noise and tile height
+ * and per 128 jobs); EBSD_BATCH_QUEUE_ALL puts every job in the queue.  With EBSD_BATCH_GRAPH all of it
  * (queue reset, launches) is captured in a CUDA graph on first use and
  * replayed for later batches with the same job list (the same buffers, sizes
  * and epilogues: new contents of the buffers are picked up).  Runs on h's
